@@ -1,0 +1,285 @@
+/*
+ * pphpc_gb300 -- C ABI of the GB300-native PPHPC simulation step.
+ *
+ * Every entry point takes plain C types and pointers; no CUDA or framework
+ * type crosses this boundary except where a function name says "dev" (a raw
+ * device address as `void*`) or "stream" (a `cudaStream_t` passed as `void*`).
+ * All functions return 0 (PP_SUCCESS) or a negative `pp_error_codes` value;
+ * the library never calls exit().
+ *
+ * Reference interfaces replaced (paths relative to the pphpc project root):
+ *   PPParameters       opencl/pp/pp_common.in.h:129-157
+ *   PPStatistics       opencl/pp/pp_common.in.h:109-124 (sums widened to 64 bit)
+ *   pp_error_codes     opencl/pp/pp_common.in.h:87-104
+ *   pp_load_params     opencl/pp/pp_common.c:39-195
+ *   pp_stats_save      opencl/pp/pp_common.c:205-240
+ *   ppg_simulate       opencl/pp/pp_gpu.c:573-987 (split into create/step/destroy)
+ *   main (pp_gpu)      opencl/pp/pp_gpu.c:1700-1946 (see pp_main.c)
+ */
+#ifndef PPHPC_GB300_H
+#define PPHPC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Error codes: opencl/pp/pp_common.in.h:87-104, extended.             */
+/* ------------------------------------------------------------------ */
+enum pp_error_codes {
+	PP_SUCCESS = 0,
+	PP_UNKNOWN_ARGS = -1,
+	PP_INVALID_ARGS = -2,
+	PP_LIBRARY_ERROR = -3,
+	PP_UNABLE_TO_OPEN_PARAMS_FILE = -4,
+	PP_INVALID_PARAMS_FILE = -5,
+	PP_UNABLE_SAVE_STATS = -6,
+	PP_OUT_OF_RESOURCES = -8,
+	/* Extensions of this library. */
+	PP_ERR_CUDA = -9,     /* a CUDA runtime call failed                    */
+	PP_ERR_TIMEOUT = -10, /* a bounded device-side wait gave up           */
+	PP_ERR_CANCELLED = -11/* a served request was cancelled              */
+};
+
+#define PP_SHEEP_ID 0
+#define PP_WOLF_ID 1
+
+/* Simulation parameters: same fields and order as the reference struct
+ * (opencl/pp/pp_common.in.h:129-157). `grid_xy` is derived. */
+typedef struct pp_parameters {
+	uint32_t init_sheep;
+	uint32_t sheep_gain_from_food;
+	uint32_t sheep_reproduce_threshold;
+	uint32_t sheep_reproduce_prob;
+	uint32_t init_wolves;
+	uint32_t wolves_gain_from_food;
+	uint32_t wolves_reproduce_threshold;
+	uint32_t wolves_reproduce_prob;
+	uint32_t grass_restart;
+	uint32_t grid_x;
+	uint32_t grid_y;
+	uint32_t grid_xy;
+	uint32_t iters;
+} PPParameters;
+
+/* Per-iteration statistics (opencl/pp/pp_common.in.h:109-124). Row k is the
+ * state after k iterations. The energy and countdown sums are 64-bit here
+ * because the reference's 32-bit sums overflow on a 12800x12800 grid. */
+typedef struct pp_statistics {
+	uint32_t sheep;
+	uint32_t wolves;
+	uint32_t grass;    /* cells with countdown == 0                    */
+	uint32_t errors;   /* pool-overflow events (0 in a successful run) */
+	uint64_t sheep_en;
+	uint64_t wolves_en;
+	uint64_t grass_en; /* sum of grass countdowns                      */
+} PPStatistics;
+
+/* ------------------------------------------------------------------ */
+/* Parameter file and stats file (drop-in formats).                    */
+/* ------------------------------------------------------------------ */
+
+/* Parse a `KEY = int` parameters file; all 12 keys required, repeats and
+ * unknown keys rejected. Replaces pp_load_params (pp_common.c:39-195).
+ * Returns PP_UNABLE_TO_OPEN_PARAMS_FILE or PP_INVALID_PARAMS_FILE on error;
+ * a message is written to `errmsg` (may be NULL) of size `errlen`. */
+int pp_load_params(PPParameters *params, const char *filename,
+	char *errmsg, size_t errlen);
+
+/* Validate parameters against this implementation's limits (grid sides
+ * 1..65535, grid_xy < 2^28, 1 <= grass_restart <= 65535, probabilities
+ * <= 100). Returns PP_SUCCESS or PP_INVALID_ARGS. */
+int pp_params_check(const PPParameters *params, char *errmsg, size_t errlen);
+
+/* Write `n_rows` stats rows as `%d\t%d\t%d\t%f\t%f\t%f\n` (sheep, wolves,
+ * grass, mean sheep energy, mean wolf energy, mean countdown), the format
+ * of pp_stats_save (pp_common.c:205-240). Means are computed in float as
+ * the reference does. Returns PP_UNABLE_SAVE_STATS on I/O failure. */
+int pp_stats_save(const char *filename, const PPStatistics *stats,
+	uint32_t n_rows, const PPParameters *params);
+
+/* Format one stats row exactly as pp_stats_save does (no newline);
+ * returns the number of characters written (snprintf semantics). */
+int pp_stats_format_row(char *buf, size_t len, const PPStatistics *row,
+	const PPParameters *params);
+
+/* ------------------------------------------------------------------ */
+/* Single simulation (one run per launch sequence).                    */
+/* ------------------------------------------------------------------ */
+
+typedef struct pp_sim pp_sim;
+
+typedef struct pp_opts {
+	int device;             /* CUDA device ordinal (default 0)                */
+	uint32_t max_agents;    /* agent pool slots; 0 = 4 x initial agents, >= 1024 */
+	uint32_t tile_cells;    /* cells per act tile (power of 2); 0 = autotune  */
+	uint32_t sort_digit_bits; /* radix digit width 4..8; 0 = autotune         */
+	uint32_t use_graph;     /* capture each iteration as a CUDA graph (1) or not (0) */
+	uint32_t unfused;       /* 1 = reference-shaped pipeline: dense per-cell
+	                           offsets + separate grass kernel; 0 = fused tiles */
+} pp_opts;
+
+/* Fill `opts` with defaults. */
+void pp_opts_default(pp_opts *opts);
+
+/* Allocate device state and initialise grid and agents (iteration 0) on
+ * the GPU. The stats of iteration 0 are available via pp_sim_stats0.
+ * Replaces the set-up half of ppg_simulate (pp_gpu.c:573-660). */
+int pp_sim_create(const PPParameters *params, uint64_t seed,
+	const pp_opts *opts, pp_sim **out);
+
+/* Statistics of the initial state (row 0 of the stats file). */
+int pp_sim_stats0(pp_sim *sim, PPStatistics *out);
+
+/* Run `n_iters` iterations; row i of `out` receives the stats after
+ * iteration (current + i + 1). Blocks until done. Replaces the loop of
+ * ppg_simulate (pp_gpu.c:671-935). Returns PP_OUT_OF_RESOURCES if the agent
+ * pool overflowed (state is then undefined). */
+int pp_sim_step(pp_sim *sim, uint32_t n_iters, PPStatistics *out);
+
+/* Same as pp_sim_step but leaves the stats in device memory: `dev_stats`
+ * is a device pointer to `n_iters` PPStatistics rows; asynchronous on the
+ * simulation's stream (pp_sim_stream). Overflow is reported by the next
+ * pp_sim_sync. */
+int pp_sim_step_async(pp_sim *sim, uint32_t n_iters, void *dev_stats);
+
+/* Wait for the simulation's stream; returns PP_OUT_OF_RESOURCES if any
+ * earlier asynchronous step overflowed the pool. */
+int pp_sim_sync(pp_sim *sim);
+
+/* Current iteration number and live agent count. */
+int pp_sim_info(pp_sim *sim, uint32_t *iter, uint32_t *n_agents,
+	uint32_t *capacity);
+
+/* Copy the state out: agents in array order (`cell`, `en` = type<<31 |
+ * energy; `n_max` slots), grass countdowns (grid_xy values; may be NULL). */
+int pp_sim_get_state(pp_sim *sim, uint32_t *cell, uint32_t *en,
+	uint32_t n_max, uint32_t *n_agents, uint16_t *grass);
+
+/* The cudaStream_t the simulation runs on (as void*). */
+void *pp_sim_stream(pp_sim *sim);
+
+int pp_sim_destroy(pp_sim *sim);
+
+/* ------------------------------------------------------------------ */
+/* Kernel-level entry points (host buffers in and out, synchronous).   */
+/* Used to check each kernel alone against the oracle.                 */
+/* ------------------------------------------------------------------ */
+
+/* Philox4x32-10 at counters {ctr0 + i, ctr1, ctr2, ctr3}, key {k0, k1}:
+ * 4*n words out (i = 0..n-1). */
+int pp_philox_fill(uint32_t ctr0, uint32_t ctr1, uint32_t ctr2, uint32_t ctr3,
+	uint32_t k0, uint32_t k1, uint32_t n, uint32_t *out);
+
+/* Move phase of iteration `iter` (move_agent, pp_gpu.cl:744-821): agents
+ * in slot order in, moved agents out (dead ones get cell = grid_xy). */
+int pp_move_host(const PPParameters *params, uint64_t seed, uint32_t iter,
+	uint32_t n, const uint32_t *cell_in, const uint32_t *en_in,
+	uint32_t *cell_out, uint32_t *en_out);
+
+/* Stable LSD radix sort of (key, value) pairs by the low `key_bits` bits
+ * (replaces the cl_ops sort call, pp_gpu.c:826-828). digit_bits 0 = auto. */
+int pp_radix_sort_host(uint32_t n, const uint32_t *keys_in,
+	const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out,
+	uint32_t key_bits, uint32_t digit_bits);
+
+/* Dense per-cell start offsets of a cell-sorted key array: off[c] = first
+ * index with key >= c, for c = 0..n_cells (find_cell_idx,
+ * pp_gpu.cl:834-867, as a full offset table). */
+int pp_cell_offsets_host(uint32_t n, const uint32_t *sorted_keys,
+	uint32_t n_cells, uint32_t *off);
+
+/* ------------------------------------------------------------------ */
+/* Batched runs: many independent replications in one launch per step. */
+/* ------------------------------------------------------------------ */
+
+typedef struct pp_run_desc {
+	PPParameters params;   /* params.iters = iterations of this run */
+	uint64_t seed;
+} pp_run_desc;
+
+/* Called from pp_batch_run after the run's last iteration with its
+ * params.iters + 1 stats rows. */
+typedef void (*pp_stats_cb)(int run, const PPStatistics *rows,
+	uint32_t n_rows, void *user);
+
+typedef struct pp_batch_opts {
+	int device;
+	uint32_t pool_factor;   /* agent pool = pool_factor x initial agents (default 4) */
+	uint32_t tile_cells;    /* 0 = autotune */
+	uint32_t sort_digit_bits; /* 0 = autotune */
+	uint32_t use_graph;     /* 1 = CUDA graph per iteration */
+	uint32_t stats_chunk;   /* iterations between stats copies to the host */
+} pp_batch_opts;
+
+void pp_batch_opts_default(pp_batch_opts *opts);
+
+/* Run `n_runs` independent simulations to completion in one shared state:
+ * every kernel launch covers all runs. Each run's stats equal those of the
+ * same run alone. */
+int pp_batch_run(const pp_run_desc *runs, int n_runs,
+	const pp_batch_opts *opts, pp_stats_cb cb, void *user);
+
+/* ------------------------------------------------------------------ */
+/* Serving: continuous batching of arriving runs.                      */
+/* ------------------------------------------------------------------ */
+
+typedef struct pp_server pp_server;
+
+typedef struct pp_serve_opts {
+	int device;
+	uint64_t mem_budget_bytes;  /* device memory cap for resident runs   */
+	uint32_t max_runs;          /* resident-run slots                     */
+	uint32_t pool_factor;       /* agent slots per run = factor x initial */
+	uint32_t stats_chunk;       /* iterations between stats streaming     */
+} pp_serve_opts;
+
+void pp_serve_opts_default(pp_serve_opts *opts);
+
+int pp_serve_create(const pp_serve_opts *opts, pp_server **out);
+
+/* Queue a run; it is admitted when slots and memory allow. `id` receives
+ * a request id. */
+int pp_serve_submit(pp_server *srv, const pp_run_desc *run, uint64_t *id);
+
+/* Cancel a queued or resident request. */
+int pp_serve_cancel(pp_server *srv, uint64_t id);
+
+/* Advance every resident run by up to `n_iters` iterations (one shared
+ * launch sequence per iteration), admitting queued runs first. */
+int pp_serve_poll(pp_server *srv, uint32_t n_iters);
+
+typedef struct pp_serve_event {
+	uint64_t id;
+	int status;          /* PP_SUCCESS, PP_OUT_OF_RESOURCES, PP_ERR_CANCELLED */
+	uint32_t n_rows;     /* rows delivered so far for this request       */
+	uint32_t done;       /* 1 when the run has finished                  */
+} pp_serve_event;
+
+/* Copy rows [first, first + n) of request `id`'s stats (available rows
+ * only); `n_out` receives the number copied. */
+int pp_serve_read(pp_server *srv, uint64_t id, uint32_t first, uint32_t n,
+	PPStatistics *rows, uint32_t *n_out);
+
+/* Status of request `id`. */
+int pp_serve_status(pp_server *srv, uint64_t id, pp_serve_event *ev);
+
+/* Number of queued and resident runs. */
+int pp_serve_load(pp_server *srv, uint32_t *queued, uint32_t *resident);
+
+/* Release a finished request's stats. */
+int pp_serve_release(pp_server *srv, uint64_t id);
+
+int pp_serve_destroy(pp_server *srv);
+
+/* Library version string. */
+const char *pp_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PPHPC_GB300_H */

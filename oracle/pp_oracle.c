@@ -1,0 +1,367 @@
+/*
+ * pp_oracle.c -- single-threaded CPU restatement of the PPHPC step.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker for the CUDA path; never linked by
+ * the product). Parity unpinned against the reference itself: the reference
+ * has no tests or golden vectors and its cl_ops RNG is not in the tree, so
+ * this file restates the model rules with Philox draws; see pp_oracle.h for
+ * the reference lines each phase follows.
+ *
+ * Canonical step (iteration t = 1..iters), over an agent array in a defined
+ * order and a grass countdown grid:
+ *   1. move   -- slot i: energy <= 1 -> dies; else energy -= 1 and one of
+ *               5 directions (stay, x+1, x-1, y+1, y-1, per-row toroidal
+ *               wrap as in pp_gpu.cl:771-800) drawn from
+ *               Philox(ctr={i, t, MOVE, 0}).w0.
+ *   2. grass  -- countdown > 0 -> countdown - 1 (pp_gpu.cl:465).
+ *   3. sort   -- stable sort of the survivors by cell index.
+ *   4. act    -- per cell, agents in increasing (priority, slot) order,
+ *               priority = Philox({s, t, ACT, 0}).w0 for sorted slot s.
+ *               This is the sequential semantics of pp_cpu.cl:596-866
+ *               with the shuffle replaced by the priority order:
+ *               a wolf eats the first not-yet-eaten sheep of the cell
+ *               (eaten sheep may have acted already); a sheep that is not
+ *               yet eaten at its turn eats the grass if countdown == 0
+ *               (countdown := restart, energy += gain); every agent that
+ *               acts then reproduces if energy > threshold and
+ *               draw(Philox({s, t, ACT, 0}).w1, 100) < prob: the child
+ *               gets energy/2 and the parent keeps the rest. Newborns
+ *               neither act nor are eaten in their birth iteration.
+ *               Output order: walk the sorted array; emit each surviving
+ *               agent, then its newborn (if any).
+ *   5. stats  -- counts and energy sums over the output array; live grass
+ *               (countdown == 0) and the countdown sum over the grid.
+ */
+#include "pp_oracle.h"
+
+#include <stdlib.h>
+#include <string.h>
+
+/* Philox4x32-10, Salmon, Moraes, Dror, Shaw, "Parallel Random Numbers: As
+ * Easy as 1, 2, 3", SC'11: round multipliers and Weyl key increments as
+ * published there. */
+#define PH_M0 0xD2511F53u
+#define PH_M1 0xCD9E8D57u
+#define PH_W0 0x9E3779B9u
+#define PH_W1 0xBB67AE85u
+
+void ppo_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+	uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+	uint32_t k0 = key[0], k1 = key[1];
+	for (int r = 0; r < 10; r++) {
+		if (r > 0) {
+			k0 += PH_W0;
+			k1 += PH_W1;
+		}
+		uint64_t p0 = (uint64_t) PH_M0 * c0;
+		uint64_t p1 = (uint64_t) PH_M1 * c2;
+		uint32_t hi0 = (uint32_t) (p0 >> 32), lo0 = (uint32_t) p0;
+		uint32_t hi1 = (uint32_t) (p1 >> 32), lo1 = (uint32_t) p1;
+		c0 = hi1 ^ c1 ^ k0;
+		c1 = lo1;
+		c2 = hi0 ^ c3 ^ k1;
+		c3 = lo0;
+	}
+	out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+uint32_t ppo_draw(uint32_t w, uint32_t n)
+{
+	return (uint32_t) (((uint64_t) w * n) >> 32);
+}
+
+static void draw4(uint64_t seed, uint32_t id, uint32_t iter, uint32_t stream,
+	uint32_t out[4])
+{
+	uint32_t ctr[4] = {id, iter, stream, 0};
+	uint32_t key[2] = {(uint32_t) seed, (uint32_t) (seed >> 32)};
+	ppo_philox(ctr, key, out);
+}
+
+struct ppo_state {
+	ppo_params p;
+	uint64_t seed;
+	uint32_t iter;
+	uint32_t cap;
+	uint32_t n;          /* live agents */
+	uint32_t *cell, *en; /* agents in canonical order */
+	uint32_t *cell2, *en2, *cell3, *en3;
+	uint16_t *grass;
+	uint32_t *count;     /* grid_xy + 2 bucket counters for the sort */
+};
+
+static uint32_t energy_of(uint32_t en) { return en & PPO_ENERGY_MASK; }
+static uint32_t type_of(uint32_t en) { return en >> 31; }
+
+ppo_state *ppo_create(const ppo_params *p, uint64_t seed, uint32_t capacity)
+{
+	ppo_state *s = (ppo_state *) calloc(1, sizeof(*s));
+	if (!s) return NULL;
+	s->p = *p;
+	s->p.grid_xy = p->grid_x * p->grid_y;
+	s->seed = seed;
+	uint64_t n0 = (uint64_t) p->init_sheep + p->init_wolves;
+	uint64_t cells = (uint64_t) p->grid_x * p->grid_y;
+	uint64_t cap = capacity ? capacity
+		: (4 * n0 > 3 * cells ? 4 * n0 : 3 * cells) + 1024;
+	if (cap < n0) cap = n0;
+	s->cap = (uint32_t) cap;
+	uint32_t C = s->p.grid_xy;
+	s->cell = malloc(sizeof(uint32_t) * cap);
+	s->en = malloc(sizeof(uint32_t) * cap);
+	s->cell2 = malloc(sizeof(uint32_t) * cap);
+	s->en2 = malloc(sizeof(uint32_t) * cap);
+	s->cell3 = malloc(sizeof(uint32_t) * cap);
+	s->en3 = malloc(sizeof(uint32_t) * cap);
+	s->grass = malloc(sizeof(uint16_t) * (size_t) C);
+	s->count = malloc(sizeof(uint32_t) * ((size_t) C + 2));
+	if (!s->cell || !s->en || !s->cell2 || !s->en2 || !s->cell3 || !s->en3
+		|| !s->grass || !s->count) {
+		ppo_destroy(s);
+		return NULL;
+	}
+	/* Grass: alive (0) w.p. 1/2, else 1 + U[0, restart) (pp_gpu.cl:383-393). */
+	for (uint32_t c = 0; c < C; c++) {
+		uint32_t r[4];
+		draw4(seed, c, 0, PPO_STREAM_INIT_CELL, r);
+		uint32_t alive = ppo_draw(r[0], 2);
+		s->grass[c] = alive ? 0
+			: (uint16_t) (1 + ppo_draw(r[1], p->grass_restart));
+	}
+	/* Agents: sheep first, then wolves (pp_gpu.cl:415-435). */
+	for (uint32_t a = 0; a < n0; a++) {
+		uint32_t r[4];
+		draw4(seed, a, 0, PPO_STREAM_INIT_AGENT, r);
+		uint32_t x = ppo_draw(r[0], p->grid_x);
+		uint32_t y = ppo_draw(r[1], p->grid_y);
+		uint32_t wolf = a >= p->init_sheep;
+		uint32_t gain = wolf ? p->wolves_gain : p->sheep_gain;
+		uint32_t e = 1 + ppo_draw(r[2], 2 * gain);
+		s->cell[a] = y * p->grid_x + x;
+		s->en[a] = (wolf ? PPO_TYPE_BIT : 0) | e;
+	}
+	s->n = (uint32_t) n0;
+	s->iter = 0;
+	return s;
+}
+
+void ppo_destroy(ppo_state *s)
+{
+	if (!s) return;
+	free(s->cell); free(s->en); free(s->cell2); free(s->en2);
+	free(s->cell3); free(s->en3); free(s->grass); free(s->count);
+	free(s);
+}
+
+static void agent_stats(uint32_t n, const uint32_t *en, ppo_stats *st)
+{
+	for (uint32_t i = 0; i < n; i++) {
+		uint32_t e = energy_of(en[i]);
+		if (type_of(en[i])) { st->wolves++; st->wolves_en += e; }
+		else { st->sheep++; st->sheep_en += e; }
+	}
+}
+
+void ppo_stats_now(const ppo_state *s, ppo_stats *out)
+{
+	memset(out, 0, sizeof(*out));
+	agent_stats(s->n, s->en, out);
+	for (uint32_t c = 0; c < s->p.grid_xy; c++) {
+		out->grass += s->grass[c] == 0;
+		out->grass_en += s->grass[c];
+	}
+}
+
+void ppo_move(const ppo_params *p, uint64_t seed, uint32_t iter, uint32_t n,
+	const uint32_t *cell_in, const uint32_t *en_in,
+	uint32_t *cell_out, uint32_t *en_out)
+{
+	uint32_t GX = p->grid_x, GY = p->grid_y, C = p->grid_x * p->grid_y;
+	for (uint32_t i = 0; i < n; i++) {
+		uint32_t en = en_in[i];
+		uint32_t e = energy_of(en);
+		if (e <= 1) {
+			cell_out[i] = C;           /* dead: sorts after every cell */
+			en_out[i] = en & PPO_TYPE_BIT;
+			continue;
+		}
+		uint32_t r[4];
+		draw4(seed, i, iter, PPO_STREAM_MOVE, r);
+		uint32_t dir = ppo_draw(r[0], 5);
+		uint32_t x = cell_in[i] % GX, y = cell_in[i] / GX;
+		switch (dir) {
+		case 1: x = (x + 1 == GX) ? 0 : x + 1; break;
+		case 2: x = (x == 0) ? GX - 1 : x - 1; break;
+		case 3: y = (y + 1 == GY) ? 0 : y + 1; break;
+		case 4: y = (y == 0) ? GY - 1 : y - 1; break;
+		default: break;
+		}
+		cell_out[i] = y * GX + x;
+		en_out[i] = (en & PPO_TYPE_BIT) | (e - 1);
+	}
+}
+
+void ppo_sort(uint32_t n, const uint32_t *k_in, const uint32_t *v_in,
+	uint32_t *k_out, uint32_t *v_out, uint32_t max_key)
+{
+	uint32_t *cnt = calloc((size_t) max_key + 2, sizeof(uint32_t));
+	for (uint32_t i = 0; i < n; i++) cnt[k_in[i] + 1]++;
+	for (uint32_t k = 0; k <= max_key; k++) cnt[k + 1] += cnt[k];
+	for (uint32_t i = 0; i < n; i++) {
+		uint32_t pos = cnt[k_in[i]]++;
+		k_out[pos] = k_in[i];
+		v_out[pos] = v_in[i];
+	}
+	free(cnt);
+}
+
+void ppo_grass(uint32_t n_cells, uint16_t *grass)
+{
+	for (uint32_t c = 0; c < n_cells; c++)
+		if (grass[c] > 0) grass[c]--;
+}
+
+typedef struct { uint32_t prio, slot; } ord_t;
+
+static int ord_cmp(const void *a, const void *b)
+{
+	const ord_t *x = a, *y = b;
+	if (x->prio != y->prio) return x->prio < y->prio ? -1 : 1;
+	return x->slot < y->slot ? -1 : (x->slot > y->slot);
+}
+
+int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
+	uint32_t n, const uint32_t *cell, const uint32_t *en, uint16_t *grass,
+	uint32_t *cell_out, uint32_t *en_out, uint32_t cap)
+{
+	uint32_t *fin = malloc(sizeof(uint32_t) * (n ? n : 1));   /* final energy */
+	uint32_t *kid = malloc(sizeof(uint32_t) * (n ? n : 1));   /* child energy, 0 = none */
+	uint8_t *eaten = malloc(n ? n : 1);
+	ord_t *ord = malloc(sizeof(ord_t) * (n ? n : 1));
+	uint32_t *dice = malloc(sizeof(uint32_t) * (n ? n : 1));
+	uint64_t out = 0;
+	int64_t ret;
+
+	uint32_t lo = 0;
+	while (lo < n) {
+		uint32_t c = cell[lo], hi = lo;
+		while (hi < n && cell[hi] == c) hi++;
+		uint32_t m = hi - lo, S = 0, W = 0;
+		for (uint32_t j = 0; j < m; j++) {
+			uint32_t s = lo + j, r[4];
+			draw4(seed, s, iter, PPO_STREAM_ACT, r);
+			ord[j].prio = r[0];
+			ord[j].slot = s;
+			dice[s] = ppo_draw(r[1], 100);
+			fin[s] = energy_of(en[s]);
+			kid[s] = 0;
+			eaten[s] = 0;
+			if (type_of(en[s])) W++; else S++;
+		}
+		qsort(ord, m, sizeof(ord_t), ord_cmp);
+		uint32_t sb = 0, wb = 0, g = grass[c];
+		for (uint32_t j = 0; j < m; j++) {
+			uint32_t s = ord[j].slot;
+			int acts;
+			uint32_t thr, prob;
+			if (type_of(en[s])) {
+				/* Wolf k eats the k-th sheep in order, if there is one
+				 * (pp_cpu.cl:721-763). */
+				if (wb < S) fin[s] += p->wolves_gain;
+				wb++;
+				acts = 1;
+				thr = p->wolves_thr; prob = p->wolves_prob;
+			} else {
+				/* Sheep j is eaten by wolf j (if j < W); it acts iff that
+				 * wolf has not come yet: wolves before <= sheep before. */
+				acts = wb <= sb;
+				eaten[s] = sb < W;
+				sb++;
+				if (acts && g == 0) {
+					g = p->grass_restart;
+					fin[s] += p->sheep_gain;
+				}
+				thr = p->sheep_thr; prob = p->sheep_prob;
+			}
+			if (acts && fin[s] > thr && dice[s] < prob) {
+				kid[s] = fin[s] / 2;
+				fin[s] -= kid[s];
+			}
+		}
+		grass[c] = (uint16_t) g;
+		lo = hi;
+	}
+	for (uint32_t s = 0; s < n; s++) {
+		uint32_t tb = en[s] & PPO_TYPE_BIT;
+		if (!eaten[s]) {
+			if (out < cap) { cell_out[out] = cell[s]; en_out[out] = tb | fin[s]; }
+			out++;
+		}
+		if (kid[s]) {
+			if (out < cap) { cell_out[out] = cell[s]; en_out[out] = tb | kid[s]; }
+			out++;
+		}
+	}
+	ret = out > cap ? -8 : (int64_t) out;
+	free(fin); free(kid); free(eaten); free(ord); free(dice);
+	return ret;
+}
+
+int ppo_step(ppo_state *s, ppo_stats *out)
+{
+	uint32_t t = s->iter + 1, C = s->p.grid_xy;
+	ppo_move(&s->p, s->seed, t, s->n, s->cell, s->en, s->cell2, s->en2);
+	ppo_grass(C, s->grass);
+	ppo_sort(s->n, s->cell2, s->en2, s->cell3, s->en3, C);
+	uint32_t live = 0;
+	while (live < s->n && s->cell3[live] < C) live++;
+	int64_t m = ppo_act(&s->p, s->seed, t, live, s->cell3, s->en3, s->grass,
+		s->cell, s->en, s->cap);
+	s->iter = t;
+	if (m < 0) {
+		s->n = 0;
+		if (out) { memset(out, 0, sizeof(*out)); out->errors = 1; }
+		return -8;
+	}
+	s->n = (uint32_t) m;
+	if (out) ppo_stats_now(s, out);
+	return 0;
+}
+
+int ppo_run(const ppo_params *p, uint64_t seed, uint32_t iters,
+	ppo_stats *rows)
+{
+	ppo_state *s = ppo_create(p, seed, 0);
+	if (!s) return -3;
+	ppo_stats_now(s, &rows[0]);
+	int rc = 0;
+	for (uint32_t t = 1; t <= iters && rc == 0; t++)
+		rc = ppo_step(s, &rows[t]);
+	ppo_destroy(s);
+	return rc;
+}
+
+uint32_t ppo_num_agents(const ppo_state *s) { return s->n; }
+uint32_t ppo_iter(const ppo_state *s) { return s->iter; }
+
+void ppo_get_agents(const ppo_state *s, uint32_t *cell, uint32_t *en)
+{
+	memcpy(cell, s->cell, sizeof(uint32_t) * s->n);
+	memcpy(en, s->en, sizeof(uint32_t) * s->n);
+}
+
+void ppo_get_grass(const ppo_state *s, uint16_t *grass)
+{
+	memcpy(grass, s->grass, sizeof(uint16_t) * s->p.grid_xy);
+}
+
+void ppo_philox_fill(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+	uint32_t k0, uint32_t k1, uint32_t n, uint32_t *out)
+{
+	uint32_t key[2] = {k0, k1};
+	for (uint32_t i = 0; i < n; i++) {
+		uint32_t ctr[4] = {c0 + i, c1, c2, c3};
+		ppo_philox(ctr, key, out + 4 * (size_t) i);
+	}
+}

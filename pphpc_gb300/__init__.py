@@ -1,0 +1,400 @@
+"""pphpc_gb300 -- GB300-native PPHPC simulation step behind a C ABI.
+
+This module is a thin ctypes mirror of ``include/pphpc.h`` (the library's
+C ABI). It loads ``libpphpc_gb300.so`` built in this package directory and
+raises if the library is missing: there is no CPU fallback for the
+simulation.
+
+Reference interfaces mirrored (paths relative to the pphpc project root):
+``PPParameters``/``PPStatistics`` (opencl/pp/pp_common.in.h:109-157),
+``pp_load_params`` (opencl/pp/pp_common.c:39-195), ``pp_stats_save``
+(opencl/pp/pp_common.c:205-240), the pp_gpu simulation loop
+(opencl/pp/pp_gpu.c:573-987).
+"""
+import ctypes as C
+import os
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libpphpc_gb300.so")
+CLI_PATH = os.path.join(_PKG, "pp_gb300")
+
+PP_SUCCESS = 0
+PP_UNKNOWN_ARGS = -1
+PP_INVALID_ARGS = -2
+PP_LIBRARY_ERROR = -3
+PP_UNABLE_TO_OPEN_PARAMS_FILE = -4
+PP_INVALID_PARAMS_FILE = -5
+PP_UNABLE_SAVE_STATS = -6
+PP_OUT_OF_RESOURCES = -8
+PP_ERR_CUDA = -9
+PP_ERR_TIMEOUT = -10
+PP_ERR_CANCELLED = -11
+
+ERROR_NAMES = {
+    0: "PP_SUCCESS", -1: "PP_UNKNOWN_ARGS", -2: "PP_INVALID_ARGS",
+    -3: "PP_LIBRARY_ERROR", -4: "PP_UNABLE_TO_OPEN_PARAMS_FILE",
+    -5: "PP_INVALID_PARAMS_FILE", -6: "PP_UNABLE_SAVE_STATS",
+    -8: "PP_OUT_OF_RESOURCES", -9: "PP_ERR_CUDA", -10: "PP_ERR_TIMEOUT",
+    -11: "PP_ERR_CANCELLED",
+}
+
+PARAM_FIELDS = ["init_sheep", "sheep_gain_from_food",
+                "sheep_reproduce_threshold", "sheep_reproduce_prob",
+                "init_wolves", "wolves_gain_from_food",
+                "wolves_reproduce_threshold", "wolves_reproduce_prob",
+                "grass_restart", "grid_x", "grid_y", "grid_xy", "iters"]
+
+
+class PPError(RuntimeError):
+    """A library call returned a negative pp_error_codes value."""
+
+    def __init__(self, code, what=""):
+        self.code = code
+        super().__init__("%s failed: %s (%d)" % (what, ERROR_NAMES.get(code, "?"), code))
+
+
+class PPParameters(C.Structure):
+    _fields_ = [(f, C.c_uint32) for f in PARAM_FIELDS]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f in PARAM_FIELDS}
+
+
+class PPStatistics(C.Structure):
+    _fields_ = [("sheep", C.c_uint32), ("wolves", C.c_uint32),
+                ("grass", C.c_uint32), ("errors", C.c_uint32),
+                ("sheep_en", C.c_uint64), ("wolves_en", C.c_uint64),
+                ("grass_en", C.c_uint64)]
+
+    def as_tuple(self):
+        return (self.sheep, self.wolves, self.grass, self.sheep_en,
+                self.wolves_en, self.grass_en)
+
+
+class PPOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("max_agents", C.c_uint32),
+                ("tile_cells", C.c_uint32), ("sort_digit_bits", C.c_uint32),
+                ("use_graph", C.c_uint32), ("unfused", C.c_uint32)]
+
+
+class PPRunDesc(C.Structure):
+    _fields_ = [("params", PPParameters), ("seed", C.c_uint64)]
+
+
+class PPBatchOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("pool_factor", C.c_uint32),
+                ("tile_cells", C.c_uint32), ("sort_digit_bits", C.c_uint32),
+                ("use_graph", C.c_uint32), ("stats_chunk", C.c_uint32)]
+
+
+class PPServeOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("mem_budget_bytes", C.c_uint64),
+                ("max_runs", C.c_uint32), ("pool_factor", C.c_uint32),
+                ("stats_chunk", C.c_uint32)]
+
+
+class PPServeEvent(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("status", C.c_int),
+                ("n_rows", C.c_uint32), ("done", C.c_uint32)]
+
+
+STATS_CB = C.CFUNCTYPE(None, C.c_int, C.POINTER(PPStatistics), C.c_uint32,
+                       C.c_void_p)
+
+# Every function the C ABI exports: name -> (restype, argtypes).
+_P = C.POINTER
+_u32p = _P(C.c_uint32)
+ABI = {
+    "pp_load_params": (C.c_int, [_P(PPParameters), C.c_char_p, C.c_char_p, C.c_size_t]),
+    "pp_params_check": (C.c_int, [_P(PPParameters), C.c_char_p, C.c_size_t]),
+    "pp_stats_save": (C.c_int, [C.c_char_p, _P(PPStatistics), C.c_uint32, _P(PPParameters)]),
+    "pp_stats_format_row": (C.c_int, [C.c_char_p, C.c_size_t, _P(PPStatistics), _P(PPParameters)]),
+    "pp_opts_default": (None, [_P(PPOpts)]),
+    "pp_sim_create": (C.c_int, [_P(PPParameters), C.c_uint64, _P(PPOpts), _P(C.c_void_p)]),
+    "pp_sim_stats0": (C.c_int, [C.c_void_p, _P(PPStatistics)]),
+    "pp_sim_step": (C.c_int, [C.c_void_p, C.c_uint32, _P(PPStatistics)]),
+    "pp_sim_step_async": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
+    "pp_sim_sync": (C.c_int, [C.c_void_p]),
+    "pp_sim_info": (C.c_int, [C.c_void_p, _u32p, _u32p, _u32p]),
+    "pp_sim_get_state": (C.c_int, [C.c_void_p, _u32p, _u32p, C.c_uint32, _u32p, _P(C.c_uint16)]),
+    "pp_sim_stream": (C.c_void_p, [C.c_void_p]),
+    "pp_sim_destroy": (C.c_int, [C.c_void_p]),
+    "pp_philox_fill": (C.c_int, [C.c_uint32] * 7 + [_u32p]),
+    "pp_move_host": (C.c_int, [_P(PPParameters), C.c_uint64, C.c_uint32, C.c_uint32,
+                               _u32p, _u32p, _u32p, _u32p]),
+    "pp_radix_sort_host": (C.c_int, [C.c_uint32, _u32p, _u32p, _u32p, _u32p,
+                                     C.c_uint32, C.c_uint32]),
+    "pp_cell_offsets_host": (C.c_int, [C.c_uint32, _u32p, C.c_uint32, _u32p]),
+    "pp_batch_opts_default": (None, [_P(PPBatchOpts)]),
+    "pp_batch_run": (C.c_int, [_P(PPRunDesc), C.c_int, _P(PPBatchOpts), STATS_CB, C.c_void_p]),
+    "pp_serve_opts_default": (None, [_P(PPServeOpts)]),
+    "pp_serve_create": (C.c_int, [_P(PPServeOpts), _P(C.c_void_p)]),
+    "pp_serve_submit": (C.c_int, [C.c_void_p, _P(PPRunDesc), _P(C.c_uint64)]),
+    "pp_serve_cancel": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "pp_serve_poll": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "pp_serve_read": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32,
+                                _P(PPStatistics), _u32p]),
+    "pp_serve_status": (C.c_int, [C.c_void_p, C.c_uint64, _P(PPServeEvent)]),
+    "pp_serve_load": (C.c_int, [C.c_void_p, _u32p, _u32p]),
+    "pp_serve_release": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "pp_serve_destroy": (C.c_int, [C.c_void_p]),
+    "pp_version": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the library (once). Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libpphpc_gb300.so is not built; run "
+                               "`python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in ABI.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc, what):
+    if rc != PP_SUCCESS:
+        raise PPError(rc, what)
+
+
+def make_params(**kw):
+    p = PPParameters()
+    for k, v in kw.items():
+        setattr(p, k, v)
+    p.grid_xy = p.grid_x * p.grid_y
+    return p
+
+
+def load_params(filename):
+    """Parse a reference parameters file (`KEY = int`, 12 keys)."""
+    p = PPParameters()
+    msg = C.create_string_buffer(256)
+    rc = lib().pp_load_params(C.byref(p), filename.encode(), msg, 256)
+    if rc != PP_SUCCESS:
+        raise PPError(rc, "pp_load_params: %s" % msg.value.decode())
+    return p
+
+
+def stats_save(filename, rows, params):
+    arr = (PPStatistics * len(rows))(*rows)
+    _check(lib().pp_stats_save(filename.encode(), arr, len(rows), C.byref(params)),
+           "pp_stats_save")
+
+
+def format_row(row, params):
+    buf = C.create_string_buffer(256)
+    lib().pp_stats_format_row(buf, 256, C.byref(row), C.byref(params))
+    return buf.value.decode()
+
+
+class Simulation:
+    """One PPHPC run on the GPU (pp_sim_* of the C ABI)."""
+
+    def __init__(self, params, seed=0, device=0, max_agents=0, tile_cells=0,
+                 digit_bits=0, use_graph=True):
+        L = lib()
+        o = PPOpts()
+        L.pp_opts_default(C.byref(o))
+        o.device = device
+        o.max_agents = max_agents
+        o.tile_cells = tile_cells
+        o.sort_digit_bits = digit_bits
+        o.use_graph = 1 if use_graph else 0
+        self.params = params
+        self._h = C.c_void_p()
+        _check(L.pp_sim_create(C.byref(params), seed, C.byref(o), C.byref(self._h)),
+               "pp_sim_create")
+
+    def stats0(self):
+        s = PPStatistics()
+        _check(lib().pp_sim_stats0(self._h, C.byref(s)), "pp_sim_stats0")
+        return s
+
+    def step(self, n):
+        rows = (PPStatistics * max(n, 1))()
+        _check(lib().pp_sim_step(self._h, n, rows), "pp_sim_step")
+        return list(rows)[:n]
+
+    def info(self):
+        it, na, cap = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        _check(lib().pp_sim_info(self._h, C.byref(it), C.byref(na), C.byref(cap)),
+               "pp_sim_info")
+        return it.value, na.value, cap.value
+
+    def state(self):
+        import numpy as np
+        _, n, _ = self.info()
+        cell = np.zeros(max(n, 1), np.uint32)
+        en = np.zeros(max(n, 1), np.uint32)
+        grass = np.zeros(self.params.grid_x * self.params.grid_y, np.uint16)
+        nout = C.c_uint32()
+        _check(lib().pp_sim_get_state(
+            self._h, cell.ctypes.data_as(_u32p), en.ctypes.data_as(_u32p), n,
+            C.byref(nout), grass.ctypes.data_as(_P(C.c_uint16))), "pp_sim_get_state")
+        return cell[:nout.value], en[:nout.value], grass
+
+    def close(self):
+        if self._h:
+            lib().pp_sim_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def run(params, seed=0, iters=None, **kw):
+    """Run a simulation; returns iters+1 stats rows (row 0 = initial)."""
+    iters = params.iters if iters is None else iters
+    with Simulation(params, seed, **kw) as sim:
+        return [sim.stats0()] + sim.step(iters)
+
+
+def batch_run(runs, pool_factor=4, tile_cells=0, digit_bits=0, use_graph=True,
+              stats_chunk=1024, device=0):
+    """Run many independent simulations in one world. `runs` is a list of
+    (PPParameters, seed); returns a list of row lists."""
+    L = lib()
+    descs = (PPRunDesc * len(runs))()
+    for i, (p, s) in enumerate(runs):
+        descs[i].params = p
+        descs[i].seed = s
+    o = PPBatchOpts()
+    L.pp_batch_opts_default(C.byref(o))
+    o.device = device
+    o.pool_factor = pool_factor
+    o.tile_cells = tile_cells
+    o.sort_digit_bits = digit_bits
+    o.use_graph = 1 if use_graph else 0
+    o.stats_chunk = stats_chunk
+    out = [None] * len(runs)
+
+    def cb(r, rows, n, user):
+        out[r] = [PPStatistics.from_buffer_copy(rows[i]) for i in range(n)]
+
+    ccb = STATS_CB(cb)
+    _check(L.pp_batch_run(descs, len(runs), C.byref(o), ccb, None), "pp_batch_run")
+    return out
+
+
+class Server:
+    """Continuous-batching server (pp_serve_* of the C ABI)."""
+
+    def __init__(self, mem_budget_bytes=8 << 30, max_runs=256, pool_factor=4,
+                 stats_chunk=64, device=0):
+        L = lib()
+        o = PPServeOpts()
+        L.pp_serve_opts_default(C.byref(o))
+        o.device = device
+        o.mem_budget_bytes = mem_budget_bytes
+        o.max_runs = max_runs
+        o.pool_factor = pool_factor
+        o.stats_chunk = stats_chunk
+        self._h = C.c_void_p()
+        _check(L.pp_serve_create(C.byref(o), C.byref(self._h)), "pp_serve_create")
+
+    def submit(self, params, seed):
+        d = PPRunDesc()
+        d.params = params
+        d.seed = seed
+        rid = C.c_uint64()
+        _check(lib().pp_serve_submit(self._h, C.byref(d), C.byref(rid)), "pp_serve_submit")
+        return rid.value
+
+    def cancel(self, rid):
+        _check(lib().pp_serve_cancel(self._h, rid), "pp_serve_cancel")
+
+    def poll(self, n_iters):
+        _check(lib().pp_serve_poll(self._h, n_iters), "pp_serve_poll")
+
+    def status(self, rid):
+        ev = PPServeEvent()
+        _check(lib().pp_serve_status(self._h, rid, C.byref(ev)), "pp_serve_status")
+        return ev
+
+    def load(self):
+        q, r = C.c_uint32(), C.c_uint32()
+        _check(lib().pp_serve_load(self._h, C.byref(q), C.byref(r)), "pp_serve_load")
+        return q.value, r.value
+
+    def read(self, rid, first=0, n=None):
+        ev = self.status(rid)
+        n = ev.n_rows - first if n is None else n
+        rows = (PPStatistics * max(n, 1))()
+        got = C.c_uint32()
+        _check(lib().pp_serve_read(self._h, rid, first, n, rows, C.byref(got)),
+               "pp_serve_read")
+        return list(rows)[:got.value]
+
+    def release(self, rid):
+        _check(lib().pp_serve_release(self._h, rid), "pp_serve_release")
+
+    def close(self):
+        if self._h:
+            lib().pp_serve_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def philox_fill(ctr, key, n):
+    import numpy as np
+    out = np.zeros(4 * n, np.uint32)
+    _check(lib().pp_philox_fill(ctr[0], ctr[1], ctr[2], ctr[3], key[0], key[1], n,
+                                out.ctypes.data_as(_u32p)), "pp_philox_fill")
+    return out.reshape(n, 4)
+
+
+def move(params, seed, it, cell, en):
+    import numpy as np
+    cell = np.ascontiguousarray(cell, np.uint32)
+    en = np.ascontiguousarray(en, np.uint32)
+    co = np.zeros_like(cell)
+    eo = np.zeros_like(en)
+    _check(lib().pp_move_host(C.byref(params), seed, it, len(cell),
+                              cell.ctypes.data_as(_u32p), en.ctypes.data_as(_u32p),
+                              co.ctypes.data_as(_u32p), eo.ctypes.data_as(_u32p)),
+           "pp_move_host")
+    return co, eo
+
+
+def radix_sort(keys, vals, key_bits, digit_bits=0):
+    import numpy as np
+    keys = np.ascontiguousarray(keys, np.uint32)
+    vals = np.ascontiguousarray(vals, np.uint32)
+    ko = np.zeros_like(keys)
+    vo = np.zeros_like(vals)
+    _check(lib().pp_radix_sort_host(len(keys), keys.ctypes.data_as(_u32p),
+                                    vals.ctypes.data_as(_u32p), ko.ctypes.data_as(_u32p),
+                                    vo.ctypes.data_as(_u32p), key_bits, digit_bits),
+           "pp_radix_sort_host")
+    return ko, vo
+
+
+def cell_offsets(sorted_keys, n_cells):
+    import numpy as np
+    k = np.ascontiguousarray(sorted_keys, np.uint32)
+    off = np.zeros(n_cells + 1, np.uint32)
+    _check(lib().pp_cell_offsets_host(len(k), k.ctypes.data_as(_u32p), n_cells,
+                                      off.ctypes.data_as(_u32p)), "pp_cell_offsets_host")
+    return off

@@ -1,0 +1,95 @@
+"""Build the pphpc_gb300 shared library, the pp_gb300 command-line tool and
+the CPU oracle (test infrastructure).
+
+Every CUDA translation unit is compiled for sm_103a only
+(`-gencode arch=compute_103a,code=sm_103a`), in parallel, then linked with
+the host C code into ``pphpc_gb300/libpphpc_gb300.so`` (CUDA runtime linked
+statically). Builds are incremental on file modification times.
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+OBJ = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libpphpc_gb300.so")
+CLI = os.path.join(PKG, "pp_gb300")
+ORACLE_SRC = os.path.join(ROOT, "oracle", "pp_oracle.c")
+ORACLE_LIB = os.path.join(ROOT, "oracle", "_build", "libpp_oracle.so")
+
+NVCC = os.environ.get("NVCC", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+                  "-Xcompiler", "-Wall"]
+CU_SOURCES = ["pp_kernels.cu", "pp_radix.cu", "pp_world.cu", "pp_serve.cu"]
+C_SOURCES = ["pp_host.c"]
+HEADERS = ["pp_device.cuh", "pp_kernels.cuh", "pp_block.cuh", "pp_world.cuh"]
+
+
+def _newer(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def _run(cmd):
+    p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                       text=True)
+    if p.returncode != 0:
+        raise RuntimeError("build failed: %s\n%s" % (" ".join(cmd), p.stdout))
+    return p.stdout
+
+
+def build_library(verbose=False, extra_nvflags=()):
+    os.makedirs(OBJ, exist_ok=True)
+    hdrs = [os.path.join(CSRC, h) for h in HEADERS]
+    hdrs.append(os.path.join(ROOT, "include", "pphpc.h"))
+    jobs = []
+    objs = []
+    for src in CU_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OBJ, src.replace(".cu", ".o"))
+        objs.append(o)
+        if _newer(o, [s] + hdrs):
+            jobs.append([NVCC] + NVFLAGS + list(extra_nvflags) + ["-c", s, "-o", o])
+    for src in C_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OBJ, src.replace(".c", ".o"))
+        objs.append(o)
+        if _newer(o, [s] + hdrs):
+            jobs.append(["gcc", "-O2", "-std=c11", "-fPIC", "-Wall", "-c", s, "-o", o])
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        for out in ex.map(_run, jobs):
+            if verbose and out:
+                sys.stdout.write(out)
+    if _newer(LIB, objs):
+        _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs)
+    main_c = os.path.join(CSRC, "pp_main.c")
+    if _newer(CLI, [main_c, LIB]):
+        _run(["gcc", "-O2", "-std=gnu11", "-Wall", "-o", CLI, main_c,
+              "-L" + PKG, "-lpphpc_gb300", "-Wl,-rpath,$ORIGIN"])
+    return LIB
+
+
+def build_oracle():
+    os.makedirs(os.path.dirname(ORACLE_LIB), exist_ok=True)
+    hdr = os.path.join(ROOT, "oracle", "pp_oracle.h")
+    if _newer(ORACLE_LIB, [ORACLE_SRC, hdr]):
+        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-Wall",
+              "-o", ORACLE_LIB, ORACLE_SRC])
+    return ORACLE_LIB
+
+
+def build_all(verbose=False):
+    lib = build_library(verbose=verbose)
+    build_oracle()
+    return lib
+
+
+if __name__ == "__main__":
+    build_all(verbose="-v" in sys.argv)
+    print(LIB)

@@ -1,0 +1,647 @@
+/*
+ * pp_kernels.cu -- the per-iteration simulation kernels for sm_103a.
+ *
+ *   k_move        move_agent (opencl/pp/pp_gpu.cl:744-821) plus the digit
+ *                 histograms of every radix pass (replaces the upfront
+ *                 histogram pass of the sort).
+ *   k_offsets     find_cell_idx (pp_gpu.cl:834-867): start index of every
+ *                 bucket (a tile of cells, or a single cell) in the
+ *                 cell-sorted agent array.
+ *   k_act         grass (pp_gpu.cl:448-476) + action_agent
+ *                 (pp_gpu.cl:883-979) + reduce_grass1/2 and
+ *                 reduce_agent1/2 (pp_gpu.cl:485-736), fused per tile of
+ *                 cells: countdown, in-cell conflict resolution in priority
+ *                 order, newborn slots by a block prefix sum, compaction of
+ *                 survivors and newborns with a decoupled look-back across
+ *                 tiles, and the stats (warp shuffles, one atomic per
+ *                 field per block and run).
+ *   k_init_*      init_cell / init_agent (pp_gpu.cl:368-439).
+ *
+ * Every kernel is grid-stride or ticket-persistent and reads its sizes
+ * from device memory, so one iteration is a fixed launch sequence that is
+ * captured once as a CUDA graph.
+ */
+#include "pp_kernels.cuh"
+#include "pp_block.cuh"
+
+namespace pp {
+
+/* ------------------------------------------------------------------ */
+/* Move                                                                */
+/* ------------------------------------------------------------------ */
+
+/* Energy loss, death and toroidal random walk of one agent
+ * (pp_gpu.cl:756-819; per-row wrap as there). */
+__device__ __forceinline__ void move_one(const RunDev &run, uint32_t key,
+	uint32_t val, uint32_t id, uint32_t t, uint32_t dead_key,
+	uint32_t &nk, uint32_t &nv)
+{
+	uint32_t e = val & ENERGY_MASK;
+	if (e <= 1) {
+		nk = dead_key;
+		nv = val & TYPE_BIT;
+		return;
+	}
+	u4 r = rng(run.seed_lo, run.seed_hi, id, t, STREAM_MOVE);
+	uint32_t dir = draw(r.x, 5);
+	uint32_t lc = key - run.cbase;
+	uint32_t y = fastdiv_div(lc, run.gxdiv);
+	uint32_t x = lc - y * run.gx;
+	if (dir == 1) x = (x + 1 == run.gx) ? 0 : x + 1;
+	else if (dir == 2) x = (x == 0) ? run.gx - 1 : x - 1;
+	else if (dir == 3) y = (y + 1 == run.gy) ? 0 : y + 1;
+	else if (dir == 4) y = (y == 0) ? run.gy - 1 : y - 1;
+	nk = run.cbase + y * run.gx + x;
+	nv = val - 1;
+}
+
+__device__ __forceinline__ bool run_live(const RunDev &run, uint32_t t)
+{
+	return run.active && t >= 1 && t <= run.iters;
+}
+
+__global__ void __launch_bounds__(256) k_move(WorldDev w)
+{
+	extern __shared__ uint32_t sh_hist[];
+	const uint32_t d = w.digit_bits, P = w.passes, mask = (1u << d) - 1;
+	for (uint32_t q = threadIdx.x; q < (P << d); q += blockDim.x)
+		sh_hist[q] = 0;
+	__syncthreads();
+	const uint32_t n = w.ctr->n_agents;
+	const uint32_t g = w.ctr->giter + 1;
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t stride = gridDim.x * blockDim.x;
+	for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+		uint32_t i = base + threadIdx.x;
+		bool valid = i < n;
+		uint32_t nk = 0xffffffffu, nv;
+		if (valid) {
+			uint32_t key = w.kA[i], val = w.vA[i];
+			uint32_t r = w.tile_run[key >> w.log_tile];
+			const RunDev &run = w.runs[r];
+			uint32_t t = g - run.start_giter;
+			if (run_live(run, t)) {
+				move_one(run, key, val, i - w.run_base[r], t, w.dead_key,
+					nk, nv);
+			} else {
+				nk = w.dead_key;
+				nv = val & TYPE_BIT;
+			}
+			w.kB[i] = nk;
+			w.vB[i] = nv;
+		}
+		/* Warp-aggregated digit counts: the array is nearly cell-sorted,
+		 * so the high digits of a warp mostly coincide. */
+		for (uint32_t p = 0; p < P; p++) {
+			uint32_t dig = valid ? ((nk >> (p * d)) & mask) : 0xffffffffu;
+			uint32_t peers = __match_any_sync(0xffffffffu, dig);
+			if (valid && lane == (uint32_t) (__ffs(peers) - 1))
+				atomicAdd(&sh_hist[(p << d) + dig], __popc(peers));
+		}
+	}
+	__syncthreads();
+	for (uint32_t q = threadIdx.x; q < (P << d); q += blockDim.x) {
+		uint32_t c = sh_hist[q];
+		if (c) atomicAdd(&w.hist[(q >> d) * 256 + (q & mask)], c);
+	}
+}
+
+/* Move of one run alone (kernel-level check): slot i has id i. */
+__global__ void k_move_only(const uint32_t *kin, const uint32_t *vin,
+	uint32_t *kout, uint32_t *vout, uint32_t n, const RunDev *run_dev,
+	uint32_t t, uint32_t dead_key)
+{
+	const RunDev run = *run_dev;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+		i += gridDim.x * blockDim.x) {
+		uint32_t nk, nv;
+		move_one(run, kin[i], vin[i], i, t, dead_key, nk, nv);
+		kout[i] = nk;
+		vout[i] = nv;
+	}
+}
+
+/* ------------------------------------------------------------------ */
+/* Bucket offsets                                                      */
+/* ------------------------------------------------------------------ */
+
+/* off[b] = first index whose key >> log_tile >= b, for b = 0..n_buckets.
+ * Keys are sorted; keys >> log_tile above n_buckets clamp to n_buckets.
+ * Each index writes the offsets of the buckets between its predecessor's
+ * bucket and its own, so every entry is written exactly once. */
+__global__ void k_offsets(const uint32_t *keys, const uint32_t *n_dev,
+	uint32_t log_tile, uint32_t n_buckets, uint32_t *off)
+{
+	const uint32_t n = *n_dev;
+	const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+	if (n == 0) {
+		for (uint32_t b = tid; b <= n_buckets; b += gridDim.x * blockDim.x)
+			off[b] = 0;
+		return;
+	}
+	for (uint32_t i = tid; i < n; i += gridDim.x * blockDim.x) {
+		uint32_t b = min(keys[i] >> log_tile, n_buckets);
+		uint32_t lo = (i == 0) ? 0 : min(keys[i - 1] >> log_tile, n_buckets) + 1;
+		for (uint32_t q = lo; q <= b; q++) off[q] = i;
+		if (i == n - 1)
+			for (uint32_t q = b + 1; q <= n_buckets; q++) off[q] = n;
+	}
+}
+
+/* ------------------------------------------------------------------ */
+/* Act                                                                 */
+/* ------------------------------------------------------------------ */
+
+/* Actions of the agents of one cell, slots [p, e) of the tile's agent
+ * list, in increasing (priority, slot) order. This is the sequential
+ * semantics of pp_cpu.cl:640-848 (wolves eat the first not-yet-eaten
+ * sheep of the cell; a sheep acts only if not eaten before its turn; the
+ * first acting sheep takes live grass; every acting agent may reproduce)
+ * in closed form: the k-th wolf eats the k-th sheep, and a sheep acts iff
+ * the wolves before it are no more than the sheep before it.
+ * On return LV[j] holds type | final energy (energy 0 = eaten) and LD[j]
+ * the newborn's energy (0 = none); on entry LD[j] holds the dice. */
+__device__ __forceinline__ void act_cell(uint32_t p, uint32_t e,
+	uint32_t *LV, const uint32_t *LP, uint32_t *LD, const RunDev &run,
+	uint32_t &g)
+{
+	uint32_t S = 0, W = 0;
+	for (uint32_t j = p; j < e; j++) {
+		if (LV[j] & TYPE_BIT) W++;
+		else S++;
+	}
+	uint32_t sb = 0, wb = 0;
+	uint32_t lp = 0;
+	uint32_t ls = 0xffffffffu; /* none selected yet */
+	const uint32_t m = e - p;
+	for (uint32_t step = 0; step < m; step++) {
+		uint32_t best = p;
+		if (m > 1) {
+			uint32_t bp = 0xffffffffu;
+			bool found = false;
+			for (uint32_t j = p; j < e; j++) {
+				uint32_t pj = LP[j];
+				bool after = (ls == 0xffffffffu) || pj > lp
+					|| (pj == lp && j > ls);
+				if (after && (!found || pj < bp)) {
+					best = j;
+					bp = pj;
+					found = true;
+				}
+			}
+		}
+		uint32_t v = LV[best];
+		uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
+		uint32_t dice = LD[best];
+		bool acts, eaten = false;
+		uint32_t thr, prob;
+		if (tb) {
+			if (wb < S) en += run.wolves_gain;
+			wb++;
+			acts = true;
+			thr = run.wolves_thr;
+			prob = run.wolves_prob;
+		} else {
+			acts = wb <= sb;
+			eaten = sb < W;
+			sb++;
+			if (acts && g == 0) {
+				g = run.restart;
+				en += run.sheep_gain;
+			}
+			thr = run.sheep_thr;
+			prob = run.sheep_prob;
+		}
+		uint32_t kid = 0;
+		if (acts && en > thr && dice < prob) {
+			kid = en >> 1;
+			en -= kid;
+		}
+		LV[best] = tb | (eaten ? 0u : en);
+		LD[best] = kid;
+		lp = LP[best];
+		ls = best;
+	}
+}
+
+/* First index in a[0, m) with a[i] >= x. */
+__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *a,
+	uint32_t m, uint32_t x)
+{
+	uint32_t lo = 0, hi = m;
+	while (lo < hi) {
+		uint32_t mid = (lo + hi) >> 1;
+		if (a[mid] < x) lo = mid + 1;
+		else hi = mid;
+	}
+	return lo;
+}
+
+struct StatAcc {
+	uint32_t sheep, wolves, galive;
+	uint64_t sen, wen, gen;
+	__device__ void zero() { sheep = wolves = galive = 0; sen = wen = gen = 0; }
+};
+
+/* Block-reduce the per-thread stats and add them to the run's stats row
+ * with one atomic per field. Must be called by all threads of the block. */
+__device__ void flush_stats(StatAcc &a, PPStatistics *dst)
+{
+	__shared__ uint64_t red[6][ACT_THREADS / 32];
+	uint64_t v[6] = {a.sheep, a.wolves, a.galive, a.sen, a.wen, a.gen};
+	const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+	for (int f = 0; f < 6; f++) {
+		v[f] = warp_sum(v[f]);
+		if (lane == 0) red[f][wid] = v[f];
+	}
+	__syncthreads();
+	if (threadIdx.x < 6) {
+		uint64_t s = 0;
+		for (uint32_t q = 0; q < ACT_THREADS / 32; q++) s += red[threadIdx.x][q];
+		if (s) {
+			switch (threadIdx.x) {
+			case 0: atomicAdd(&dst->sheep, (uint32_t) s); break;
+			case 1: atomicAdd(&dst->wolves, (uint32_t) s); break;
+			case 2: atomicAdd(&dst->grass, (uint32_t) s); break;
+			case 3: atomicAdd((unsigned long long *) &dst->sheep_en, s); break;
+			case 4: atomicAdd((unsigned long long *) &dst->wolves_en, s); break;
+			default: atomicAdd((unsigned long long *) &dst->grass_en, s); break;
+			}
+		}
+	}
+	__syncthreads();
+	a.zero();
+}
+
+template <int CPT>
+__global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
+	const uint32_t *__restrict__ kS, uint32_t *__restrict__ vS)
+{
+	extern __shared__ uint32_t sm[];
+	uint32_t *sk = sm, *sv = sm + w.act_cap, *sp = sv + w.act_cap,
+		*sd = sp + w.act_cap;
+	__shared__ uint32_t s_tile, s_base, s_last;
+	const uint32_t tid = threadIdx.x;
+	const uint32_t giter = w.ctr->giter;
+	const uint32_t g = giter + 1;
+	const uint32_t epoch = w.ctr->seq * 8u + 7u;
+	const uint32_t row = g % w.ring_rows;
+	StatAcc acc;
+	acc.zero();
+	int cur_run = -1;
+
+	for (;;) {
+		if (tid == 0) s_tile = atomicAdd(&w.ctr->act_ticket, 1u);
+		__syncthreads();
+		const uint32_t tile = s_tile;
+		if (tile >= w.n_tiles) break;
+		const uint32_t r = w.tile_run[tile];
+		if ((int) r != cur_run) {
+			if (cur_run >= 0)
+				flush_stats(acc, &w.ring[(size_t) row * w.nruns_cap + cur_run]);
+			cur_run = (int) r;
+		}
+		const RunDev run = w.runs[r];
+		const uint32_t t = g - run.start_giter;
+		const bool live = run_live(run, t);
+		const uint32_t c0 = tile << w.log_tile;
+		const uint32_t a0 = w.tile_off[tile], a1 = w.tile_off[tile + 1];
+		const uint32_t m = a1 - a0;
+		const uint32_t sbase = w.tile_off[run.first_tile];
+		const bool in_smem = m <= w.act_cap;
+		uint32_t *LK, *LV, *LP, *LD;
+		if (in_smem) {
+			LK = sk; LV = sv; LP = sp; LD = sd;
+		} else {
+			LK = const_cast<uint32_t *>(kS) + a0;
+			LV = vS + a0;
+			LP = w.scratch_prio + a0;
+			LD = w.scratch_kid + a0;
+		}
+		for (uint32_t j = tid; j < m; j += ACT_THREADS) {
+			uint32_t k = kS[a0 + j], v = vS[a0 + j];
+			if (in_smem) {
+				sk[j] = k;
+				sv[j] = v;
+			}
+			u4 rr = rng(run.seed_lo, run.seed_hi, a0 + j - sbase, t,
+				STREAM_ACT);
+			LP[j] = rr.x;
+			LD[j] = draw(rr.y, 100);
+		}
+		/* Grass of this thread's CPT cells (vector load). */
+		const uint32_t cell0 = tid * CPT;
+		uint16_t gr[CPT];
+		uint16_t *gp = w.grass + c0 + cell0;
+		if (CPT == 8) {
+			uint4 q = *reinterpret_cast<const uint4 *>(gp);
+			memcpy(gr, &q, 16);
+		} else if (CPT == 4) {
+			uint2 q = *reinterpret_cast<const uint2 *>(gp);
+			memcpy(gr, &q, 8);
+		} else {
+#pragma unroll
+			for (int q = 0; q < CPT; q += 8) {
+				uint4 v = *reinterpret_cast<const uint4 *>(gp + q);
+				memcpy(gr + q, &v, 16);
+			}
+		}
+		__syncthreads();
+		const uint32_t lc0 = c0 - run.cbase + cell0;
+		const uint32_t pbeg = lower_bound_u32(LK, m, c0 + cell0);
+		const uint32_t pend = lower_bound_u32(LK, m, c0 + cell0 + CPT);
+		uint32_t p = pbeg;
+#pragma unroll
+		for (int q = 0; q < CPT; q++) {
+			const uint32_t cell = c0 + cell0 + q;
+			const bool real = live && (lc0 + q) < run.ncells;
+			uint32_t gq = gr[q];
+			if (real && gq > 0) gq--;
+			uint32_t e = p;
+			while (e < pend && LK[e] == cell) e++;
+			if (e > p) {
+				if (real) {
+					act_cell(p, e, LV, LP, LD, run, gq);
+				} else {
+					for (uint32_t j = p; j < e; j++) {
+						LV[j] &= TYPE_BIT;
+						LD[j] = 0;
+					}
+				}
+			}
+			if (real) {
+				acc.galive += gq == 0;
+				acc.gen += gq;
+			}
+			gr[q] = (uint16_t) gq;
+			p = e;
+		}
+		/* Survivors + newborns of this thread, in slot order. */
+		uint32_t cnt = 0;
+		for (uint32_t j = pbeg; j < pend; j++)
+			cnt += ((LV[j] & ENERGY_MASK) != 0) + (LD[j] != 0);
+		uint32_t total;
+		const uint32_t excl = block_excl_scan(cnt, &total);
+		if (tid == 0) {
+			uint32_t base = lookback(w.lb_act, 1, tile, total, epoch,
+				&w.ctr->err);
+			s_base = base;
+			if (tile == run.first_tile) w.run_base[r] = base;
+			if (tile == w.n_tiles - 1)
+				w.ctr->n_agents = min(base + total, w.cap);
+		}
+		__syncthreads();
+		uint32_t o = s_base + excl;
+		for (uint32_t j = pbeg; j < pend; j++) {
+			const uint32_t v = LV[j], k = LK[j], kd = LD[j];
+			const uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
+			if (en) {
+				if (o < w.cap) {
+					w.kA[o] = k;
+					w.vA[o] = v;
+				}
+				o++;
+				if (tb) { acc.wolves++; acc.wen += en; }
+				else { acc.sheep++; acc.sen += en; }
+			}
+			if (kd) {
+				if (o < w.cap) {
+					w.kA[o] = k;
+					w.vA[o] = tb | kd;
+				}
+				o++;
+				if (tb) { acc.wolves++; acc.wen += kd; }
+				else { acc.sheep++; acc.sen += kd; }
+			}
+		}
+		if (o > w.cap) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
+		if (live) {
+			if (CPT == 8) {
+				uint4 q;
+				memcpy(&q, gr, 16);
+				*reinterpret_cast<uint4 *>(gp) = q;
+			} else if (CPT == 4) {
+				uint2 q;
+				memcpy(&q, gr, 8);
+				*reinterpret_cast<uint2 *>(gp) = q;
+			} else {
+#pragma unroll
+				for (int q = 0; q < CPT; q += 8) {
+					uint4 v;
+					memcpy(&v, gr + q, 16);
+					*reinterpret_cast<uint4 *>(gp + q) = v;
+				}
+			}
+		}
+		__syncthreads();
+	}
+	if (cur_run >= 0)
+		flush_stats(acc, &w.ring[(size_t) row * w.nruns_cap + cur_run]);
+
+	/* The last CTA to finish advances the iteration and resets the
+	 * per-launch counters and accumulators for the next iteration. */
+	__threadfence();
+	__syncthreads();
+	if (tid == 0) {
+		s_last = 0;
+		uint32_t done = atomicAdd(&w.ctr->act_done, 1u);
+		if (done == gridDim.x - 1) {
+			__threadfence();
+			s_last = 1;
+			w.ctr->giter = g;
+			w.ctr->seq = w.ctr->seq + 1;
+			w.ctr->act_ticket = 0;
+			w.ctr->act_done = 0;
+			for (int q = 0; q < 8; q++) w.ctr->sort_ticket[q] = 0;
+		}
+	}
+	__syncthreads();
+	if (s_last) {
+		for (uint32_t q = tid; q < 8 * 256; q += ACT_THREADS) w.hist[q] = 0;
+		const uint32_t nrow = (g + 1) % w.ring_rows;
+		uint32_t *rowp = reinterpret_cast<uint32_t *>(
+			&w.ring[(size_t) nrow * w.nruns_cap]);
+		const uint32_t words = w.nruns_cap * (sizeof(PPStatistics) / 4);
+		for (uint32_t q = tid; q < words; q += ACT_THREADS) rowp[q] = 0;
+	}
+}
+
+/* ------------------------------------------------------------------ */
+/* Init and stats of a freshly initialised run                         */
+/* ------------------------------------------------------------------ */
+
+__global__ void k_init_grass(WorldDev w, RunDev run)
+{
+	const uint32_t span = run.n_tiles << w.log_tile;
+	for (uint32_t lc = blockIdx.x * blockDim.x + threadIdx.x; lc < span;
+		lc += gridDim.x * blockDim.x) {
+		uint16_t v = 0;
+		if (lc < run.ncells) {
+			u4 r = rng(run.seed_lo, run.seed_hi, lc, 0, STREAM_INIT_CELL);
+			uint32_t alive = draw(r.x, 2);
+			v = alive ? 0 : (uint16_t) (1 + draw(r.y, run.restart));
+		}
+		w.grass[run.cbase + lc] = v;
+	}
+}
+
+__global__ void k_init_agents(WorldDev w, RunDev run, uint32_t base,
+	uint32_t n_sheep, uint32_t n_wolves)
+{
+	const uint32_t n = n_sheep + n_wolves;
+	for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < n;
+		a += gridDim.x * blockDim.x) {
+		u4 r = rng(run.seed_lo, run.seed_hi, a, 0, STREAM_INIT_AGENT);
+		uint32_t x = draw(r.x, run.gx), y = draw(r.y, run.gy);
+		bool wolf = a >= n_sheep;
+		uint32_t gain = wolf ? run.wolves_gain : run.sheep_gain;
+		uint32_t e = 1 + draw(r.z, 2 * gain);
+		w.kA[base + a] = run.cbase + y * run.gx + x;
+		w.vA[base + a] = (wolf ? TYPE_BIT : 0u) | e;
+	}
+}
+
+/* Stats of a run's current state: agents A[base, base + n), its cells. */
+__global__ void __launch_bounds__(ACT_THREADS) k_stats_run(WorldDev w,
+	RunDev run, uint32_t base, uint32_t n, PPStatistics *dst)
+{
+	StatAcc acc;
+	acc.zero();
+	const uint32_t stride = gridDim.x * blockDim.x;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+		uint32_t v = w.vA[base + i], en = v & ENERGY_MASK;
+		if (v & TYPE_BIT) { acc.wolves++; acc.wen += en; }
+		else { acc.sheep++; acc.sen += en; }
+	}
+	for (uint32_t lc = blockIdx.x * blockDim.x + threadIdx.x; lc < run.ncells;
+		lc += stride) {
+		uint32_t gq = w.grass[run.cbase + lc];
+		acc.galive += gq == 0;
+		acc.gen += gq;
+	}
+	flush_stats(acc, dst);
+}
+
+__global__ void k_philox_fill(uint32_t c0, uint32_t c1, uint32_t c2,
+	uint32_t c3, uint32_t k0, uint32_t k1, uint32_t n, uint32_t *out)
+{
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+		i += gridDim.x * blockDim.x) {
+		u4 r = philox4x32_10(u4{c0 + i, c1, c2, c3}, k0, k1);
+		reinterpret_cast<uint4 *>(out)[i] = make_uint4(r.x, r.y, r.z, r.w);
+	}
+}
+
+/* ------------------------------------------------------------------ */
+/* Host-side launch wrappers                                           */
+/* ------------------------------------------------------------------ */
+
+cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
+	cudaStream_t s)
+{
+	size_t hist_smem = (size_t) (w.passes << w.digit_bits) * sizeof(uint32_t);
+	k_move<<<lc.move_blocks, 256, hist_smem, s>>>(w);
+	uint32_t *ki = w.kB, *vi = w.vB, *ko = w.kC, *vo = w.vC;
+	for (uint32_t p = 0; p < w.passes; p++) {
+		cudaError_t e = launch_radix_pass(ki, vi, ko, vo, w.hist + p * 256,
+			w.lb_sort, w.ctr, &w.ctr->n_agents, p, p * w.digit_bits,
+			w.digit_bits, lc.sort_blocks, s);
+		if (e != cudaSuccess) return e;
+		uint32_t *tk = ki, *tv = vi;
+		ki = ko; vi = vo; ko = tk; vo = tv;
+	}
+	/* ki/vi now hold the cell-sorted agents (dead ones last). */
+	k_offsets<<<lc.offs_blocks, 256, 0, s>>>(ki, &w.ctr->n_agents,
+		w.log_tile, w.n_tiles, w.tile_off);
+	size_t act_smem = (size_t) w.act_cap * 4 * sizeof(uint32_t);
+	switch (lc.cpt) {
+	case 4: k_act<4><<<lc.act_blocks, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
+	case 16: k_act<16><<<lc.act_blocks, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
+	default: k_act<8><<<lc.act_blocks, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
+	}
+	return cudaGetLastError();
+}
+
+cudaError_t set_act_smem_limits(size_t bytes)
+{
+	cudaError_t e;
+	e = cudaFuncSetAttribute(k_act<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+	if (e != cudaSuccess) return e;
+	e = cudaFuncSetAttribute(k_act<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+	if (e != cudaSuccess) return e;
+	return cudaFuncSetAttribute(k_act<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+}
+
+cudaError_t enqueue_init_run(const WorldDev &w, const LaunchCfg &lc,
+	const RunDev &run, uint32_t r, uint32_t base, uint32_t init_sheep,
+	uint32_t init_wolves, uint32_t row, cudaStream_t s)
+{
+	(void) lc;
+	uint32_t span = run.n_tiles << w.log_tile;
+	uint32_t gb = (span + 255) / 256;
+	if (gb > 4096) gb = 4096;
+	k_init_grass<<<gb, 256, 0, s>>>(w, run);
+	uint32_t n = init_sheep + init_wolves;
+	if (n) {
+		uint32_t ab = (n + 255) / 256;
+		if (ab > 4096) ab = 4096;
+		k_init_agents<<<ab, 256, 0, s>>>(w, run, base, init_sheep, init_wolves);
+	}
+	uint32_t sb = (max(n, run.ncells) + ACT_THREADS - 1) / ACT_THREADS;
+	if (sb > 1024) sb = 1024;
+	if (sb == 0) sb = 1;
+	k_stats_run<<<sb, ACT_THREADS, 0, s>>>(w, run, base, n,
+		&w.ring[(size_t) row * w.nruns_cap + r]);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_move_only(const uint32_t *kin, const uint32_t *vin,
+	uint32_t *kout, uint32_t *vout, uint32_t n, const RunDev *run_dev,
+	uint32_t iter, uint32_t dead_key, cudaStream_t s)
+{
+	uint32_t b = (n + 255) / 256;
+	if (b > 4096) b = 4096;
+	if (b == 0) b = 1;
+	k_move_only<<<b, 256, 0, s>>>(kin, vin, kout, vout, n, run_dev, iter,
+		dead_key);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_offsets(const uint32_t *keys, const uint32_t *n_dev,
+	uint32_t log_tile, uint32_t n_buckets, uint32_t *off, int blocks,
+	cudaStream_t s)
+{
+	k_offsets<<<blocks, 256, 0, s>>>(keys, n_dev, log_tile, n_buckets, off);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_philox_fill(uint32_t c0, uint32_t c1, uint32_t c2,
+	uint32_t c3, uint32_t k0, uint32_t k1, uint32_t n, uint32_t *out,
+	cudaStream_t s)
+{
+	uint32_t b = (n + 255) / 256;
+	if (b > 4096) b = 4096;
+	if (b == 0) b = 1;
+	k_philox_fill<<<b, 256, 0, s>>>(c0, c1, c2, c3, k0, k1, n, out);
+	return cudaGetLastError();
+}
+
+} /* namespace pp */
+
+namespace pp {
+
+int occupancy_act(int cpt, size_t smem)
+{
+	int n = 0;
+	cudaError_t e;
+	switch (cpt) {
+	case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_act<4>, ACT_THREADS, smem); break;
+	case 16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_act<16>, ACT_THREADS, smem); break;
+	default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_act<8>, ACT_THREADS, smem); break;
+	}
+	if (e != cudaSuccess) { cudaGetLastError(); return 1; }
+	return n;
+}
+
+} /* namespace pp */

@@ -1,0 +1,81 @@
+/*
+ * pp_kernels.cuh -- launch wrappers of the simulation kernels (defined in
+ * pp_kernels.cu and pp_radix.cu).
+ */
+#pragma once
+
+#include "pp_device.cuh"
+#include "../../include/pphpc.h"
+
+namespace pp {
+
+/* Everything one world iteration touches. Arrays A, B, C are agent
+ * key/value arrays of `cap` slots: A = pre-move (canonical order), the
+ * move writes B, the radix passes ping-pong B <-> C, the act reads the
+ * sorted array and writes A. */
+struct WorldDev {
+	uint16_t *grass;          /* n_tiles << log_tile cells                 */
+	uint32_t *kA, *vA, *kB, *vB, *kC, *vC;
+	uint32_t *tile_off;       /* n_tiles + 1                               */
+	uint16_t *tile_run;       /* n_tiles                                   */
+	RunDev *runs;             /* nruns_cap                                 */
+	uint32_t *run_base;       /* agent base of each run in A               */
+	uint64_t *lb_sort;        /* sort look-back words [max sort tiles][radix] */
+	uint64_t *lb_act;         /* act look-back words [n_tiles]             */
+	WorldCounters *ctr;
+	uint32_t *hist;           /* [8][256] digit counts of the moved keys   */
+	PPStatistics *ring;       /* [ring_rows][nruns_cap]                    */
+	uint32_t *scratch_prio, *scratch_kid; /* [cap], act fallback           */
+	uint32_t cap, n_tiles, log_tile, nruns_cap, ring_rows;
+	uint32_t key_bits, digit_bits, passes;
+	uint32_t act_cap;         /* agents per tile held in shared memory     */
+	uint32_t dead_key;        /* = n_tiles << log_tile                      */
+};
+
+struct LaunchCfg {
+	int sms;
+	int move_blocks, sort_blocks, act_blocks, offs_blocks;
+	int cpt;                  /* cells per act thread (4, 8 or 16)          */
+};
+
+/* Sort tile geometry. */
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_IPT = 16;
+constexpr int SORT_TILE = SORT_THREADS * SORT_IPT;
+constexpr int ACT_THREADS = 256;
+
+/* One iteration: move, radix passes, tile offsets, act. Returns a CUDA
+ * error code (cudaSuccess = 0). */
+cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
+	cudaStream_t s);
+
+/* Initialise run r: grass of its tiles, its initial agents at A[base..),
+ * and accumulate its initial stats into ring row `row`. */
+cudaError_t enqueue_init_run(const WorldDev &w, const LaunchCfg &lc,
+	const RunDev &run, uint32_t r, uint32_t base, uint32_t init_sheep,
+	uint32_t init_wolves, uint32_t row, cudaStream_t s);
+
+/* Standalone kernels for kernel-level checks. */
+cudaError_t launch_move_only(const uint32_t *kin, const uint32_t *vin,
+	uint32_t *kout, uint32_t *vout, uint32_t n, const RunDev *run_dev,
+	uint32_t iter, uint32_t dead_key, cudaStream_t s);
+
+cudaError_t launch_offsets(const uint32_t *keys, const uint32_t *n_dev,
+	uint32_t log_tile, uint32_t n_buckets, uint32_t *off, int blocks,
+	cudaStream_t s);
+
+cudaError_t launch_philox_fill(uint32_t c0, uint32_t c1, uint32_t c2,
+	uint32_t c3, uint32_t k0, uint32_t k1, uint32_t n, uint32_t *out,
+	cudaStream_t s);
+
+/* Radix sort primitives (pp_radix.cu). */
+cudaError_t launch_radix_hist(const uint32_t *keys, const uint32_t *n_dev,
+	uint32_t *hist, uint32_t digit_bits, uint32_t passes, int blocks,
+	cudaStream_t s);
+
+cudaError_t launch_radix_pass(const uint32_t *kin, const uint32_t *vin,
+	uint32_t *kout, uint32_t *vout, const uint32_t *hist_pass,
+	uint64_t *lb, WorldCounters *ctr, const uint32_t *n_dev, uint32_t pass,
+	uint32_t shift, uint32_t digit_bits, int blocks, cudaStream_t s);
+
+} /* namespace pp */

@@ -1,0 +1,130 @@
+/*
+ * pp_main.c -- command-line drop-in for the reference's pp_gpu executable
+ * (opencl/pp/pp_gpu.c:1700-1946, options pp_gpu.c:310-410).
+ *
+ *   pp_gb300 [-p PARAMS] [-s STATS] [-r SEED] [-d DEVICE] [-m MAX_AGENTS]
+ *            [--iters N] [-i PROF_FILE] [-t TILE] [--digit-bits B]
+ *            [--no-graph]
+ *
+ * -p/-s/-r/-d/-m keep the reference's meaning and defaults (config.txt,
+ * stats.txt, seed 0, device 0, agent pool); --iters overrides ITERS from
+ * the parameters file (the reference has no such knob: -i there is the
+ * profiling export, kept here as a two-column kernel-time file). The
+ * exit status is a pp_error_codes value, as in the reference.
+ */
+#include <getopt.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "../../include/pphpc.h"
+
+static double now_s(void)
+{
+	struct timespec ts;
+	clock_gettime(CLOCK_MONOTONIC, &ts);
+	return ts.tv_sec + ts.tv_nsec * 1e-9;
+}
+
+static void usage(const char *argv0)
+{
+	fprintf(stderr,
+		"Usage: %s [-p FILE] [-s FILE] [-r SEED] [-d INDEX] [-m MAX]\n"
+		"          [--iters N] [-i FILE] [-t TILE] [--digit-bits B] [--no-graph]\n",
+		argv0);
+}
+
+int main(int argc, char **argv)
+{
+	const char *params_file = NULL, *stats_file = NULL, *prof_file = NULL;
+	long long seed = 0;
+	long long iters_override = -1;
+	pp_opts opts;
+	pp_opts_default(&opts);
+	static struct option longopts[] = {
+		{"params", required_argument, 0, 'p'},
+		{"stats", required_argument, 0, 's'},
+		{"rng-seed", required_argument, 0, 'r'},
+		{"device", required_argument, 0, 'd'},
+		{"max-agents", required_argument, 0, 'm'},
+		{"prof-agg", required_argument, 0, 'i'},
+		{"iters", required_argument, 0, 'I'},
+		{"tile", required_argument, 0, 't'},
+		{"digit-bits", required_argument, 0, 'D'},
+		{"no-graph", no_argument, 0, 'G'},
+		{"help", no_argument, 0, 'h'},
+		{0, 0, 0, 0}
+	};
+	int c;
+	while ((c = getopt_long(argc, argv, "p:s:r:d:m:i:t:h", longopts, NULL)) != -1) {
+		switch (c) {
+		case 'p': params_file = optarg; break;
+		case 's': stats_file = optarg; break;
+		case 'r': seed = strtoll(optarg, NULL, 0); break;
+		case 'd': opts.device = atoi(optarg); break;
+		case 'm': opts.max_agents = (uint32_t) strtoul(optarg, NULL, 0); break;
+		case 'i': prof_file = optarg; break;
+		case 'I': iters_override = strtoll(optarg, NULL, 0); break;
+		case 't': opts.tile_cells = (uint32_t) strtoul(optarg, NULL, 0); break;
+		case 'D': opts.sort_digit_bits = (uint32_t) strtoul(optarg, NULL, 0); break;
+		case 'G': opts.use_graph = 0; break;
+		case 'h': usage(argv[0]); return PP_SUCCESS;
+		default: usage(argv[0]); return PP_UNKNOWN_ARGS;
+		}
+	}
+	if (optind < argc) {
+		fprintf(stderr, "Error: This program does not accept non-option arguments.\n");
+		return PP_UNKNOWN_ARGS;
+	}
+	char msg[256] = "";
+	PPParameters params;
+	int rc = pp_load_params(&params, params_file, msg, sizeof(msg));
+	if (rc) {
+		fprintf(stderr, "Error: %s\n", msg);
+		return rc;
+	}
+	if (iters_override >= 0) params.iters = (uint32_t) iters_override;
+	rc = pp_params_check(&params, msg, sizeof(msg));
+	if (rc) {
+		fprintf(stderr, "Error: %s\n", msg);
+		return rc;
+	}
+	PPStatistics *rows = (PPStatistics *) calloc((size_t) params.iters + 1,
+		sizeof(PPStatistics));
+	if (!rows) return PP_OUT_OF_RESOURCES;
+	double t0 = now_s();
+	pp_sim *sim = NULL;
+	rc = pp_sim_create(&params, (uint64_t) seed, &opts, &sim);
+	if (rc) {
+		fprintf(stderr, "Error: unable to create simulation (%d)\n", rc);
+		free(rows);
+		return rc;
+	}
+	pp_sim_stats0(sim, &rows[0]);
+	double t1 = now_s();
+	rc = pp_sim_step(sim, params.iters, rows + 1);
+	double t2 = now_s();
+	if (rc == PP_OUT_OF_RESOURCES)
+		fprintf(stderr, "Error: agents required above the pool limit "
+			"(-m); raise it\n");
+	else if (rc)
+		fprintf(stderr, "Error: simulation failed (%d)\n", rc);
+	pp_sim_destroy(sim);
+	if (rc == PP_SUCCESS) {
+		rc = pp_stats_save(stats_file, rows, params.iters + 1, &params);
+		if (rc) fprintf(stderr, "Error: unable to save stats\n");
+	}
+	if (rc == PP_SUCCESS && prof_file) {
+		FILE *fp = fopen(prof_file, "w");
+		if (fp) {
+			fprintf(fp, "\"init\"\t%.0f\n\"simulate\"\t%.0f\n",
+				(t1 - t0) * 1e9, (t2 - t1) * 1e9);
+			fclose(fp);
+		}
+	}
+	if (rc == PP_SUCCESS)
+		printf("Ellapsed time: %.4es\n", t2 - t0);
+	free(rows);
+	return rc;
+}

@@ -1,0 +1,774 @@
+/*
+ * pp_world.cu -- world management and the C ABI of single simulations,
+ * batched runs and kernel-level entry points.
+ *
+ * The reference's host loop (opencl/pp/pp_gpu.c:573-987) blocks on the
+ * host every iteration to read the stats and size the next launches
+ * (pp_gpu.c:840-852). Here every kernel reads its sizes from device
+ * counters, so an iteration is a fixed launch sequence; `graph_iters`
+ * iterations are captured once into a CUDA graph and replayed, and the
+ * host synchronises only every `ring_rows - 1` iterations to copy the
+ * stats ring out and check the overflow/timeout flags.
+ */
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <new>
+
+#include "pp_world.cuh"
+
+namespace pp {
+
+cudaError_t set_act_smem_limits(size_t bytes);
+int occupancy_act(int cpt, size_t smem);
+int occupancy_sort(int dbits);
+
+int cuda_status(cudaError_t e)
+{
+	if (e == cudaSuccess) return PP_SUCCESS;
+	if (e == cudaErrorMemoryAllocation) return PP_OUT_OF_RESOURCES;
+	return PP_ERR_CUDA;
+}
+
+#define PP_CK(call) do { cudaError_t e_ = (call); \
+	if (e_ != cudaSuccess) return cuda_status(e_); } while (0)
+
+static uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t) ((a + b - 1) / b); }
+
+static uint32_t pow2_ceil(uint32_t v)
+{
+	uint32_t p = 1;
+	while (p < v) p <<= 1;
+	return p;
+}
+
+void choose_geometry(uint32_t total_cells, uint32_t cap, WorldConfig &cfg)
+{
+	if (cfg.tile_cells == 0) {
+		/* Dense worlds (many agents per cell) take smaller tiles so a
+		 * tile's agents fit in shared memory. */
+		double dens = total_cells ? (double) cap / total_cells : 1.0;
+		cfg.tile_cells = dens > 1.0 ? 1024 : 2048;
+	}
+	(void) cap;
+}
+
+World::~World() { free_all(); }
+
+void World::free_all()
+{
+	if (device_ >= 0 && !allocs_.empty()) cudaSetDevice(device_);
+	if (gexec_) cudaGraphExecDestroy(gexec_);
+	if (graph_) cudaGraphDestroy(graph_);
+	gexec_ = nullptr;
+	graph_ = nullptr;
+	for (void *p : allocs_) cudaFree(p);
+	allocs_.clear();
+	if (s_) cudaStreamDestroy(s_);
+	s_ = nullptr;
+}
+
+int World::alloc(size_t bytes, void **p)
+{
+	if (bytes == 0) bytes = 16;
+	cudaError_t e = cudaMalloc(p, bytes);
+	if (e != cudaSuccess) {
+		cudaGetLastError();
+		return e == cudaErrorMemoryAllocation ? PP_OUT_OF_RESOURCES : PP_ERR_CUDA;
+	}
+	allocs_.push_back(*p);
+	bytes_ += bytes;
+	return PP_SUCCESS;
+}
+
+static RunDev make_run(const RunSpec &s, uint32_t first_tile,
+	uint32_t n_tiles, uint32_t log_tile, uint32_t start_giter)
+{
+	RunDev r{};
+	r.gx = s.p.grid_x;
+	r.gy = s.p.grid_y;
+	r.ncells = s.p.grid_x * s.p.grid_y;
+	r.cbase = first_tile << log_tile;
+	r.first_tile = first_tile;
+	r.n_tiles = n_tiles;
+	r.sheep_gain = s.p.sheep_gain_from_food;
+	r.sheep_thr = s.p.sheep_reproduce_threshold;
+	r.sheep_prob = s.p.sheep_reproduce_prob;
+	r.wolves_gain = s.p.wolves_gain_from_food;
+	r.wolves_thr = s.p.wolves_reproduce_threshold;
+	r.wolves_prob = s.p.wolves_reproduce_prob;
+	r.restart = s.p.grass_restart;
+	r.seed_lo = (uint32_t) s.seed;
+	r.seed_hi = (uint32_t) (s.seed >> 32);
+	r.iters = s.iters;
+	r.start_giter = start_giter;
+	r.active = 1;
+	r.gxdiv = fastdiv_make(s.p.grid_x);
+	return r;
+}
+
+int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
+{
+	WorldConfig cfg = cfg_in;
+	device_ = cfg.device;
+	PP_CK(cudaSetDevice(device_));
+	PP_CK(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
+	int sms = 0;
+	PP_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+
+	uint64_t total_cells = 0, n0 = 0;
+	for (const RunSpec &r : runs) {
+		total_cells += (uint64_t) r.p.grid_x * r.p.grid_y;
+		n0 += (uint64_t) r.p.init_sheep + r.p.init_wolves;
+	}
+	if (cfg.cap == 0) cfg.cap = (uint32_t) std::min<uint64_t>(
+		std::max<uint64_t>(4 * n0, 1024), 0x7fffffffu);
+	if (n0 > cfg.cap) return PP_OUT_OF_RESOURCES;
+	choose_geometry((uint32_t) std::min<uint64_t>(total_cells, 0xffffffffu),
+		cfg.cap, cfg);
+	uint32_t T = cfg.tile_cells;
+	if (T != 1024 && T != 2048 && T != 4096) return PP_INVALID_ARGS;
+	uint32_t log_tile = 0;
+	while ((1u << log_tile) < T) log_tile++;
+
+	uint64_t tiles = 0;
+	std::vector<uint32_t> first(runs.size()), ntl(runs.size());
+	for (size_t r = 0; r < runs.size(); r++) {
+		uint64_t c = (uint64_t) runs[r].p.grid_x * runs[r].p.grid_y;
+		first[r] = (uint32_t) tiles;
+		ntl[r] = ceil_div(c, T);
+		tiles += ntl[r];
+	}
+	used_tiles_ = (uint32_t) tiles;
+	tiles += cfg.extra_tiles;
+	if (tiles == 0) tiles = 1;
+	if ((tiles << log_tile) >= 0x80000000ull) return PP_INVALID_ARGS;
+
+	uint32_t nruns_cap = std::max<uint32_t>(cfg.nruns_cap, (uint32_t) runs.size()) + 1;
+	null_slot_ = nruns_cap - 1;
+	if (nruns_cap > 65535) return PP_INVALID_ARGS;
+
+	w_.cap = cfg.cap;
+	w_.n_tiles = (uint32_t) tiles;
+	w_.log_tile = log_tile;
+	w_.nruns_cap = nruns_cap;
+	w_.ring_rows = std::max<uint32_t>(cfg.ring_rows, 16);
+	w_.dead_key = (uint32_t) (tiles << log_tile);
+	uint32_t kb = 32 - __builtin_clz(w_.dead_key);
+	w_.key_bits = kb;
+	uint32_t d = cfg.digit_bits;
+	if (d == 0) {
+		uint32_t passes = (kb + 7) / 8;
+		d = (kb + passes - 1) / passes;
+	}
+	if (d < 5) d = 5;
+	if (d > 8) return PP_INVALID_ARGS;
+	w_.digit_bits = d;
+	w_.passes = (kb + d - 1) / d;
+	if (w_.passes > 8) return PP_INVALID_ARGS;
+
+	uint32_t act_cap = cfg.act_cap;
+	if (act_cap == 0) {
+		double dens = total_cells ? (double) cfg.cap / (double) total_cells : 2.0;
+		if (dens > 2.0) dens = 2.0;
+		act_cap = pow2_ceil((uint32_t) (T * dens * 1.5) + 1);
+		act_cap = std::min<uint32_t>(std::max<uint32_t>(act_cap, 256), 4096);
+	}
+	w_.act_cap = act_cap;
+
+	const size_t cap = cfg.cap;
+	int rc;
+#define PP_AL(ptr, bytes) do { void *p_; rc = alloc((bytes), &p_); \
+	if (rc) return rc; (ptr) = (decltype(ptr)) p_; } while (0)
+	PP_AL(w_.grass, (size_t) w_.dead_key * sizeof(uint16_t));
+	PP_AL(w_.kA, cap * 4); PP_AL(w_.vA, cap * 4);
+	PP_AL(w_.kB, cap * 4); PP_AL(w_.vB, cap * 4);
+	PP_AL(w_.kC, cap * 4); PP_AL(w_.vC, cap * 4);
+	PP_AL(w_.scratch_prio, cap * 4); PP_AL(w_.scratch_kid, cap * 4);
+	PP_AL(w_.tile_off, ((size_t) tiles + 1) * 4);
+	PP_AL(w_.tile_run, (size_t) tiles * 2);
+	PP_AL(w_.runs, (size_t) nruns_cap * sizeof(RunDev));
+	PP_AL(w_.run_base, (size_t) nruns_cap * 4);
+	size_t sort_tiles = ceil_div(cap, SORT_TILE) + 1;
+	PP_AL(w_.lb_sort, sort_tiles * 256 * sizeof(uint64_t));
+	PP_AL(w_.lb_act, (size_t) tiles * sizeof(uint64_t));
+	PP_AL(w_.ctr, sizeof(WorldCounters));
+	PP_AL(w_.hist, 8 * 256 * 4);
+	PP_AL(w_.ring, (size_t) w_.ring_rows * nruns_cap * sizeof(PPStatistics));
+#undef PP_AL
+	PP_CK(cudaMemsetAsync(w_.lb_sort, 0, sort_tiles * 256 * sizeof(uint64_t), s_));
+	PP_CK(cudaMemsetAsync(w_.lb_act, 0, (size_t) tiles * sizeof(uint64_t), s_));
+	PP_CK(cudaMemsetAsync(w_.hist, 0, 8 * 256 * 4, s_));
+	PP_CK(cudaMemsetAsync(w_.ring, 0, (size_t) w_.ring_rows * nruns_cap * sizeof(PPStatistics), s_));
+	PP_CK(cudaMemsetAsync(w_.run_base, 0, (size_t) nruns_cap * 4, s_));
+
+	/* Run table and tile map. */
+	runs_h_.assign(nruns_cap, RunDev{});
+	reserve_of_.assign(nruns_cap, 0);
+	tile_run_h_.assign(tiles, (uint16_t) null_slot_);
+	std::vector<uint32_t> base_h(nruns_cap, 0);
+	uint32_t base = 0;
+	for (size_t r = 0; r < runs.size(); r++) {
+		runs_h_[r] = make_run(runs[r], first[r], ntl[r], log_tile, 0);
+		for (uint32_t t = 0; t < ntl[r]; t++) tile_run_h_[first[r] + t] = (uint16_t) r;
+		base_h[r] = base;
+		base += runs[r].p.init_sheep + runs[r].p.init_wolves;
+	}
+	if (cfg.extra_tiles) free_tiles_.push_back({used_tiles_, cfg.extra_tiles});
+	PP_CK(cudaMemcpyAsync(w_.runs, runs_h_.data(), nruns_cap * sizeof(RunDev), cudaMemcpyHostToDevice, s_));
+	PP_CK(cudaMemcpyAsync(w_.tile_run, tile_run_h_.data(), tiles * 2, cudaMemcpyHostToDevice, s_));
+	PP_CK(cudaMemcpyAsync(w_.run_base, base_h.data(), nruns_cap * 4, cudaMemcpyHostToDevice, s_));
+	WorldCounters c{};
+	c.n_agents = base;
+	PP_CK(cudaMemcpyAsync(w_.ctr, &c, sizeof(c), cudaMemcpyHostToDevice, s_));
+
+	/* Launch geometry. */
+	lc_.sms = sms;
+	lc_.cpt = (int) (T / ACT_THREADS);
+	size_t act_smem = (size_t) act_cap * 16;
+	PP_CK(set_act_smem_limits(act_smem));
+	int occ_act = occupancy_act(lc_.cpt, act_smem);
+	int occ_sort = occupancy_sort((int) d);
+	if (occ_act < 1) occ_act = 1;
+	if (occ_sort < 1) occ_sort = 1;
+	lc_.act_blocks = (int) std::min<uint64_t>(tiles, (uint64_t) sms * occ_act);
+	lc_.sort_blocks = sms * occ_sort;
+	lc_.move_blocks = sms * 8;
+	lc_.offs_blocks = sms * 8;
+
+	for (size_t r = 0; r < runs.size(); r++) {
+		rc = cuda_status(enqueue_init_run(w_, lc_, runs_h_[r], (uint32_t) r,
+			base_h[r], runs[r].p.init_sheep, runs[r].p.init_wolves, 0, s_));
+		if (rc) return rc;
+	}
+	giter_ = 0;
+	graph_iters_ = cfg.graph_iters;
+	PP_CK(cudaStreamSynchronize(s_));
+	if (graph_iters_) {
+		rc = build_graph();
+		if (rc) return rc;
+	}
+	return PP_SUCCESS;
+}
+
+int World::build_graph()
+{
+	if (gexec_) { cudaGraphExecDestroy(gexec_); gexec_ = nullptr; }
+	if (graph_) { cudaGraphDestroy(graph_); graph_ = nullptr; }
+	PP_CK(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
+	for (uint32_t i = 0; i < graph_iters_; i++) {
+		cudaError_t e = enqueue_iteration(w_, lc_, s_);
+		if (e != cudaSuccess) {
+			cudaGraph_t g;
+			cudaStreamEndCapture(s_, &g);
+			if (g) cudaGraphDestroy(g);
+			return cuda_status(e);
+		}
+	}
+	PP_CK(cudaStreamEndCapture(s_, &graph_));
+	PP_CK(cudaGraphInstantiate(&gexec_, graph_, 0));
+	return PP_SUCCESS;
+}
+
+int World::enqueue(uint32_t n)
+{
+	PP_CK(cudaSetDevice(device_));
+	uint32_t done = 0;
+	if (gexec_ && graph_iters_) {
+		while (n - done >= graph_iters_) {
+			PP_CK(cudaGraphLaunch(gexec_, s_));
+			done += graph_iters_;
+		}
+	}
+	for (; done < n; done++) PP_CK(enqueue_iteration(w_, lc_, s_));
+	giter_ += n;
+	return PP_SUCCESS;
+}
+
+int World::sync_check()
+{
+	PP_CK(cudaSetDevice(device_));
+	PP_CK(cudaStreamSynchronize(s_));
+	uint32_t err = 0;
+	PP_CK(cudaMemcpy(&err, &w_.ctr->err, 4, cudaMemcpyDeviceToHost));
+	if (err & ERRF_TIMEOUT) return PP_ERR_TIMEOUT;
+	if (err & ERRF_OVERFLOW) return PP_OUT_OF_RESOURCES;
+	return PP_SUCCESS;
+}
+
+uint32_t World::n_agents_dev()
+{
+	uint32_t n = 0;
+	cudaSetDevice(device_);
+	cudaStreamSynchronize(s_);
+	cudaMemcpy(&n, &w_.ctr->n_agents, 4, cudaMemcpyDeviceToHost);
+	return n;
+}
+
+int World::read_rows(uint32_t r, uint32_t g0, uint32_t g1, PPStatistics *out)
+{
+	if (g1 < g0) return PP_SUCCESS;
+	PP_CK(cudaSetDevice(device_));
+	const uint32_t R = w_.ring_rows;
+	const size_t pitch = (size_t) w_.nruns_cap * sizeof(PPStatistics);
+	uint32_t g = g0;
+	while (g <= g1) {
+		uint32_t pos = g % R;
+		uint32_t cnt = std::min<uint32_t>(g1 - g + 1, R - pos);
+		PP_CK(cudaMemcpy2DAsync(out + (g - g0), sizeof(PPStatistics),
+			&w_.ring[(size_t) pos * w_.nruns_cap + r], pitch,
+			sizeof(PPStatistics), cnt, cudaMemcpyDeviceToHost, s_));
+		g += cnt;
+	}
+	PP_CK(cudaStreamSynchronize(s_));
+	return PP_SUCCESS;
+}
+
+int World::get_state(uint32_t *cell, uint32_t *en, uint32_t n_max,
+	uint32_t *n_out, uint16_t *grass, uint32_t r)
+{
+	PP_CK(cudaSetDevice(device_));
+	PP_CK(cudaStreamSynchronize(s_));
+	uint32_t n = 0;
+	PP_CK(cudaMemcpy(&n, &w_.ctr->n_agents, 4, cudaMemcpyDeviceToHost));
+	if (n_out) *n_out = n;
+	uint32_t m = std::min(n, n_max);
+	if (cell && m) PP_CK(cudaMemcpy(cell, w_.kA, (size_t) m * 4, cudaMemcpyDeviceToHost));
+	if (en && m) PP_CK(cudaMemcpy(en, w_.vA, (size_t) m * 4, cudaMemcpyDeviceToHost));
+	if (grass) {
+		const RunDev &run = runs_h_[r];
+		PP_CK(cudaMemcpy(grass, w_.grass + run.cbase,
+			(size_t) run.ncells * 2, cudaMemcpyDeviceToHost));
+	}
+	if (cell && m) {
+		/* Report cells relative to the run's grid. */
+		uint32_t cb = runs_h_[r].cbase;
+		for (uint32_t i = 0; i < m; i++) cell[i] -= cb;
+	}
+	return PP_SUCCESS;
+}
+
+bool World::fits(const RunSpec &spec) const
+{
+	uint32_t need = ceil_div((uint64_t) spec.p.grid_x * spec.p.grid_y,
+		1u << w_.log_tile);
+	bool tiles_ok = false;
+	for (auto &f : free_tiles_) if (f.second >= need) { tiles_ok = true; break; }
+	bool slot_ok = false;
+	for (uint32_t r = 0; r < null_slot_; r++)
+		if (!runs_h_[r].active) { slot_ok = true; break; }
+	return tiles_ok && slot_ok;
+}
+
+int World::admit(const RunSpec &spec, uint32_t *slot_out)
+{
+	PP_CK(cudaSetDevice(device_));
+	uint32_t need = ceil_div((uint64_t) spec.p.grid_x * spec.p.grid_y,
+		1u << w_.log_tile);
+	int fi = -1;
+	for (size_t i = 0; i < free_tiles_.size(); i++)
+		if (free_tiles_[i].second >= need) { fi = (int) i; break; }
+	uint32_t slot = null_slot_;
+	for (uint32_t r = 0; r < null_slot_; r++)
+		if (!runs_h_[r].active) { slot = r; break; }
+	if (fi < 0 || slot == null_slot_) return PP_OUT_OF_RESOURCES;
+	uint32_t first = free_tiles_[fi].first;
+	free_tiles_[fi].first += need;
+	free_tiles_[fi].second -= need;
+	if (free_tiles_[fi].second == 0) free_tiles_.erase(free_tiles_.begin() + fi);
+
+	PP_CK(cudaStreamSynchronize(s_));
+	uint32_t n = 0;
+	PP_CK(cudaMemcpy(&n, &w_.ctr->n_agents, 4, cudaMemcpyDeviceToHost));
+	uint32_t n0 = spec.p.init_sheep + spec.p.init_wolves;
+	if ((uint64_t) n + n0 > w_.cap) {
+		free_tiles_.push_back({first, need});
+		return PP_OUT_OF_RESOURCES;
+	}
+	RunDev run = make_run(spec, first, need, w_.log_tile, giter_);
+	runs_h_[slot] = run;
+	for (uint32_t t = 0; t < need; t++) tile_run_h_[first + t] = (uint16_t) slot;
+	PP_CK(cudaMemcpyAsync(&w_.runs[slot], &run, sizeof(RunDev), cudaMemcpyHostToDevice, s_));
+	PP_CK(cudaMemcpyAsync(&w_.tile_run[first], &tile_run_h_[first], need * 2, cudaMemcpyHostToDevice, s_));
+	PP_CK(cudaMemcpyAsync(&w_.run_base[slot], &n, 4, cudaMemcpyHostToDevice, s_));
+	uint32_t row = giter_ % w_.ring_rows;
+	PP_CK(cudaMemsetAsync(&w_.ring[(size_t) row * w_.nruns_cap + slot], 0, sizeof(PPStatistics), s_));
+	int rc = cuda_status(enqueue_init_run(w_, lc_, run, slot, n,
+		spec.p.init_sheep, spec.p.init_wolves, row, s_));
+	if (rc) return rc;
+	uint32_t nn = n + n0;
+	PP_CK(cudaMemcpyAsync(&w_.ctr->n_agents, &nn, 4, cudaMemcpyHostToDevice, s_));
+	*slot_out = slot;
+	return PP_SUCCESS;
+}
+
+int World::retire(uint32_t slot)
+{
+	PP_CK(cudaSetDevice(device_));
+	if (slot >= null_slot_ || !runs_h_[slot].active) return PP_INVALID_ARGS;
+	RunDev &run = runs_h_[slot];
+	uint32_t first = run.first_tile, cnt = run.n_tiles;
+	run.active = 0;
+	/* The run's agents die in the next move (inactive run). Its tiles go
+	 * back to the free list, mapped to the null slot. */
+	PP_CK(cudaMemcpyAsync(&w_.runs[slot], &run, sizeof(RunDev), cudaMemcpyHostToDevice, s_));
+	for (uint32_t t = 0; t < cnt; t++) tile_run_h_[first + t] = (uint16_t) null_slot_;
+	PP_CK(cudaMemcpyAsync(&w_.tile_run[first], &tile_run_h_[first], (size_t) cnt * 2,
+		cudaMemcpyHostToDevice, s_));
+	free_tiles_.push_back({first, cnt});
+	std::sort(free_tiles_.begin(), free_tiles_.end());
+	std::vector<std::pair<uint32_t, uint32_t>> merged;
+	for (auto &f : free_tiles_) {
+		if (!merged.empty() && merged.back().first + merged.back().second == f.first)
+			merged.back().second += f.second;
+		else merged.push_back(f);
+	}
+	free_tiles_.swap(merged);
+	return PP_SUCCESS;
+}
+
+} /* namespace pp */
+
+/* ==================================================================== */
+/* C ABI                                                                 */
+/* ==================================================================== */
+
+using namespace pp;
+
+extern "C" int pp_params_check(const PPParameters *p, char *errmsg, size_t errlen);
+
+struct pp_sim {
+	World world;
+	PPParameters params;
+	uint64_t seed;
+	PPStatistics stats0;
+};
+
+extern "C" void pp_opts_default(pp_opts *o)
+{
+	memset(o, 0, sizeof(*o));
+	o->device = 0;
+	o->max_agents = 0;
+	o->tile_cells = 0;
+	o->sort_digit_bits = 0;
+	o->use_graph = 1;
+	o->unfused = 0;
+}
+
+extern "C" int pp_sim_create(const PPParameters *params, uint64_t seed,
+	const pp_opts *opts, pp_sim **out)
+{
+	if (!params || !out) return PP_INVALID_ARGS;
+	*out = nullptr;
+	PPParameters p = *params;
+	p.grid_xy = p.grid_x * p.grid_y;
+	int rc = pp_params_check(&p, nullptr, 0);
+	if (rc) return rc;
+	pp_opts o;
+	if (opts) o = *opts;
+	else pp_opts_default(&o);
+	pp_sim *sim = new (std::nothrow) pp_sim();
+	if (!sim) return PP_OUT_OF_RESOURCES;
+	sim->params = p;
+	sim->seed = seed;
+	WorldConfig cfg;
+	cfg.device = o.device;
+	uint64_t n0 = (uint64_t) p.init_sheep + p.init_wolves;
+	uint64_t cap = o.max_agents ? o.max_agents
+		: std::max<uint64_t>(std::max<uint64_t>(4 * n0, 1024), 16777216ull);
+	cfg.cap = (uint32_t) std::min<uint64_t>(cap, 0x7fffffffu);
+	cfg.tile_cells = o.tile_cells;
+	cfg.digit_bits = o.sort_digit_bits;
+	cfg.graph_iters = o.use_graph ? 32 : 0;
+	std::vector<RunSpec> runs(1);
+	runs[0].p = p;
+	runs[0].seed = seed;
+	runs[0].iters = 0xffffffffu;
+	rc = sim->world.create(runs, cfg);
+	if (rc == PP_SUCCESS) rc = sim->world.read_rows(0, 0, 0, &sim->stats0);
+	if (rc) {
+		delete sim;
+		cudaGetLastError();
+		return rc;
+	}
+	*out = sim;
+	return PP_SUCCESS;
+}
+
+extern "C" int pp_sim_stats0(pp_sim *sim, PPStatistics *out)
+{
+	if (!sim || !out) return PP_INVALID_ARGS;
+	*out = sim->stats0;
+	return PP_SUCCESS;
+}
+
+extern "C" int pp_sim_step(pp_sim *sim, uint32_t n_iters, PPStatistics *out)
+{
+	if (!sim) return PP_INVALID_ARGS;
+	World &w = sim->world;
+	const uint32_t chunk_max = w.ring_rows() - 1;
+	uint32_t done = 0;
+	while (done < n_iters) {
+		uint32_t chunk = std::min(n_iters - done, chunk_max);
+		uint32_t g0 = w.giter();
+		int rc = w.enqueue(chunk);
+		if (rc) return rc;
+		rc = w.sync_check();
+		if (rc) return rc;
+		if (out) {
+			rc = w.read_rows(0, g0 + 1, g0 + chunk, out + done);
+			if (rc) return rc;
+		}
+		done += chunk;
+	}
+	return PP_SUCCESS;
+}
+
+extern "C" int pp_sim_step_async(pp_sim *sim, uint32_t n_iters, void *dev_stats)
+{
+	if (!sim) return PP_INVALID_ARGS;
+	World &w = sim->world;
+	if (n_iters >= w.ring_rows()) return PP_INVALID_ARGS;
+	uint32_t g0 = w.giter();
+	int rc = w.enqueue(n_iters);
+	if (rc) return rc;
+	if (dev_stats && n_iters) {
+		const uint32_t R = w.ring_rows();
+		const size_t pitch = (size_t) w.dev().nruns_cap * sizeof(PPStatistics);
+		uint32_t g = g0 + 1, g1 = g0 + n_iters;
+		PPStatistics *dst = (PPStatistics *) dev_stats;
+		while (g <= g1) {
+			uint32_t pos = g % R;
+			uint32_t cnt = std::min<uint32_t>(g1 - g + 1, R - pos);
+			cudaError_t e = cudaMemcpy2DAsync(dst + (g - g0 - 1),
+				sizeof(PPStatistics), &w.dev().ring[(size_t) pos * w.dev().nruns_cap],
+				pitch, sizeof(PPStatistics), cnt, cudaMemcpyDeviceToDevice,
+				w.stream());
+			if (e != cudaSuccess) return cuda_status(e);
+			g += cnt;
+		}
+	}
+	return PP_SUCCESS;
+}
+
+extern "C" int pp_sim_sync(pp_sim *sim)
+{
+	if (!sim) return PP_INVALID_ARGS;
+	return sim->world.sync_check();
+}
+
+extern "C" int pp_sim_info(pp_sim *sim, uint32_t *iter, uint32_t *n_agents,
+	uint32_t *capacity)
+{
+	if (!sim) return PP_INVALID_ARGS;
+	if (iter) *iter = sim->world.giter();
+	if (n_agents) *n_agents = sim->world.n_agents_dev();
+	if (capacity) *capacity = sim->world.dev().cap;
+	return PP_SUCCESS;
+}
+
+extern "C" int pp_sim_get_state(pp_sim *sim, uint32_t *cell, uint32_t *en,
+	uint32_t n_max, uint32_t *n_agents, uint16_t *grass)
+{
+	if (!sim) return PP_INVALID_ARGS;
+	return sim->world.get_state(cell, en, n_max, n_agents, grass, 0);
+}
+
+extern "C" void *pp_sim_stream(pp_sim *sim)
+{
+	return sim ? (void *) sim->world.stream() : nullptr;
+}
+
+extern "C" int pp_sim_destroy(pp_sim *sim)
+{
+	delete sim;
+	return PP_SUCCESS;
+}
+
+/* ---------------- kernel-level entry points ---------------- */
+
+namespace {
+
+struct DevBuf {
+	void *p = nullptr;
+	~DevBuf() { if (p) cudaFree(p); }
+	cudaError_t alloc(size_t n) { return cudaMalloc(&p, n ? n : 16); }
+	template <typename T> T *as() { return (T *) p; }
+};
+
+} /* namespace */
+
+extern "C" int pp_philox_fill(uint32_t c0, uint32_t c1, uint32_t c2,
+	uint32_t c3, uint32_t k0, uint32_t k1, uint32_t n, uint32_t *out)
+{
+	if (!out && n) return PP_INVALID_ARGS;
+	DevBuf d;
+	PP_CK(d.alloc((size_t) n * 16));
+	PP_CK(launch_philox_fill(c0, c1, c2, c3, k0, k1, n, d.as<uint32_t>(), 0));
+	PP_CK(cudaMemcpy(out, d.p, (size_t) n * 16, cudaMemcpyDeviceToHost));
+	return PP_SUCCESS;
+}
+
+extern "C" int pp_move_host(const PPParameters *params, uint64_t seed,
+	uint32_t iter, uint32_t n, const uint32_t *cell_in, const uint32_t *en_in,
+	uint32_t *cell_out, uint32_t *en_out)
+{
+	if (!params) return PP_INVALID_ARGS;
+	RunSpec s{};
+	s.p = *params;
+	s.seed = seed;
+	s.iters = 0xffffffffu;
+	RunDev run = make_run(s, 0, 1, 0, 0);
+	DevBuf ki, vi, ko, vo, rd;
+	size_t b = (size_t) n * 4;
+	PP_CK(ki.alloc(b)); PP_CK(vi.alloc(b)); PP_CK(ko.alloc(b)); PP_CK(vo.alloc(b));
+	PP_CK(rd.alloc(sizeof(RunDev)));
+	PP_CK(cudaMemcpy(ki.p, cell_in, b, cudaMemcpyHostToDevice));
+	PP_CK(cudaMemcpy(vi.p, en_in, b, cudaMemcpyHostToDevice));
+	PP_CK(cudaMemcpy(rd.p, &run, sizeof(RunDev), cudaMemcpyHostToDevice));
+	PP_CK(launch_move_only(ki.as<uint32_t>(), vi.as<uint32_t>(),
+		ko.as<uint32_t>(), vo.as<uint32_t>(), n, rd.as<RunDev>(), iter,
+		params->grid_x * params->grid_y, 0));
+	PP_CK(cudaMemcpy(cell_out, ko.p, b, cudaMemcpyDeviceToHost));
+	PP_CK(cudaMemcpy(en_out, vo.p, b, cudaMemcpyDeviceToHost));
+	return PP_SUCCESS;
+}
+
+extern "C" int pp_radix_sort_host(uint32_t n, const uint32_t *keys_in,
+	const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out,
+	uint32_t key_bits, uint32_t digit_bits)
+{
+	if (key_bits == 0 || key_bits > 32) return PP_INVALID_ARGS;
+	uint32_t d = digit_bits;
+	if (d == 0) {
+		uint32_t passes = (key_bits + 7) / 8;
+		d = (key_bits + passes - 1) / passes;
+		if (d < 5) d = 5;
+	}
+	if (d < 5 || d > 8) return PP_INVALID_ARGS;
+	uint32_t passes = (key_bits + d - 1) / d;
+	int sms = 0;
+	PP_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+	size_t b = (size_t) n * 4;
+	size_t tiles = ceil_div(n, SORT_TILE) + 1;
+	DevBuf k0, v0, k1, v1, lb, ctr, hist, nd;
+	PP_CK(k0.alloc(b)); PP_CK(v0.alloc(b)); PP_CK(k1.alloc(b)); PP_CK(v1.alloc(b));
+	PP_CK(lb.alloc(tiles * 256 * 8));
+	PP_CK(ctr.alloc(sizeof(WorldCounters)));
+	PP_CK(hist.alloc(8 * 256 * 4));
+	PP_CK(nd.alloc(4));
+	PP_CK(cudaMemset(lb.p, 0, tiles * 256 * 8));
+	PP_CK(cudaMemset(ctr.p, 0, sizeof(WorldCounters)));
+	PP_CK(cudaMemset(hist.p, 0, 8 * 256 * 4));
+	PP_CK(cudaMemcpy(nd.p, &n, 4, cudaMemcpyHostToDevice));
+	PP_CK(cudaMemcpy(k0.p, keys_in, b, cudaMemcpyHostToDevice));
+	PP_CK(cudaMemcpy(v0.p, vals_in, b, cudaMemcpyHostToDevice));
+	PP_CK(launch_radix_hist(k0.as<uint32_t>(), nd.as<uint32_t>(),
+		hist.as<uint32_t>(), d, passes, sms * 4, 0));
+	uint32_t *ki = k0.as<uint32_t>(), *vi = v0.as<uint32_t>();
+	uint32_t *ko = k1.as<uint32_t>(), *vo = v1.as<uint32_t>();
+	int occ = occupancy_sort((int) d);
+	for (uint32_t p = 0; p < passes; p++) {
+		PP_CK(launch_radix_pass(ki, vi, ko, vo, hist.as<uint32_t>() + p * 256,
+			lb.as<uint64_t>(), ctr.as<WorldCounters>(), nd.as<uint32_t>(), p,
+			p * d, d, sms * (occ > 0 ? occ : 1), 0));
+		std::swap(ki, ko);
+		std::swap(vi, vo);
+	}
+	PP_CK(cudaDeviceSynchronize());
+	WorldCounters c{};
+	PP_CK(cudaMemcpy(&c, ctr.p, sizeof(c), cudaMemcpyDeviceToHost));
+	if (c.err & ERRF_TIMEOUT) return PP_ERR_TIMEOUT;
+	PP_CK(cudaMemcpy(keys_out, ki, b, cudaMemcpyDeviceToHost));
+	PP_CK(cudaMemcpy(vals_out, vi, b, cudaMemcpyDeviceToHost));
+	return PP_SUCCESS;
+}
+
+extern "C" int pp_cell_offsets_host(uint32_t n, const uint32_t *sorted_keys,
+	uint32_t n_cells, uint32_t *off)
+{
+	int sms = 0;
+	PP_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+	DevBuf k, o, nd;
+	PP_CK(k.alloc((size_t) n * 4));
+	PP_CK(o.alloc(((size_t) n_cells + 1) * 4));
+	PP_CK(nd.alloc(4));
+	PP_CK(cudaMemcpy(k.p, sorted_keys, (size_t) n * 4, cudaMemcpyHostToDevice));
+	PP_CK(cudaMemcpy(nd.p, &n, 4, cudaMemcpyHostToDevice));
+	PP_CK(launch_offsets(k.as<uint32_t>(), nd.as<uint32_t>(), 0, n_cells,
+		o.as<uint32_t>(), sms * 8, 0));
+	PP_CK(cudaMemcpy(off, o.p, ((size_t) n_cells + 1) * 4, cudaMemcpyDeviceToHost));
+	return PP_SUCCESS;
+}
+
+/* ---------------- batched runs ---------------- */
+
+extern "C" void pp_batch_opts_default(pp_batch_opts *o)
+{
+	memset(o, 0, sizeof(*o));
+	o->pool_factor = 4;
+	o->use_graph = 1;
+	o->stats_chunk = 1024;
+}
+
+extern "C" int pp_batch_run(const pp_run_desc *runs, int n_runs,
+	const pp_batch_opts *opts, pp_stats_cb cb, void *user)
+{
+	if (!runs || n_runs <= 0) return PP_INVALID_ARGS;
+	pp_batch_opts o;
+	if (opts) o = *opts;
+	else pp_batch_opts_default(&o);
+	std::vector<RunSpec> specs(n_runs);
+	uint64_t n0 = 0, cells = 0;
+	uint32_t max_iters = 0;
+	for (int r = 0; r < n_runs; r++) {
+		PPParameters p = runs[r].params;
+		p.grid_xy = p.grid_x * p.grid_y;
+		int rc = pp_params_check(&p, nullptr, 0);
+		if (rc) return rc;
+		specs[r].p = p;
+		specs[r].seed = runs[r].seed;
+		specs[r].iters = p.iters;
+		n0 += (uint64_t) p.init_sheep + p.init_wolves;
+		cells += p.grid_xy;
+		max_iters = std::max(max_iters, p.iters);
+	}
+	WorldConfig cfg;
+	cfg.device = o.device;
+	uint32_t pf = o.pool_factor ? o.pool_factor : 4;
+	cfg.cap = (uint32_t) std::min<uint64_t>(std::max<uint64_t>(pf * n0, 1024), 0x7fffffffu);
+	cfg.tile_cells = o.tile_cells;
+	cfg.digit_bits = o.sort_digit_bits;
+	cfg.graph_iters = o.use_graph ? 32 : 0;
+	uint32_t chunk = o.stats_chunk ? o.stats_chunk : 1024;
+	cfg.ring_rows = std::max<uint32_t>(chunk + 1, 64);
+	World w;
+	int rc = w.create(specs, cfg);
+	if (rc) return rc;
+	std::vector<std::vector<PPStatistics>> rows(n_runs);
+	for (int r = 0; r < n_runs; r++) {
+		rows[r].resize((size_t) specs[r].iters + 1);
+		rc = w.read_rows((uint32_t) r, 0, 0, rows[r].data());
+		if (rc) return rc;
+	}
+	uint32_t g = 0;
+	while (g < max_iters) {
+		uint32_t c = std::min(max_iters - g, chunk);
+		rc = w.enqueue(c);
+		if (rc) return rc;
+		rc = w.sync_check();
+		if (rc) return rc;
+		for (int r = 0; r < n_runs; r++) {
+			uint32_t it = specs[r].iters;
+			if (g >= it) continue;
+			uint32_t hi = std::min(g + c, it);
+			rc = w.read_rows((uint32_t) r, g + 1, hi, rows[r].data() + g + 1);
+			if (rc) return rc;
+			if (hi == it && cb) cb(r, rows[r].data(), it + 1, user);
+		}
+		g += c;
+	}
+	if (max_iters == 0 && cb)
+		for (int r = 0; r < n_runs; r++) cb(r, rows[r].data(), 1, user);
+	return PP_SUCCESS;
+}

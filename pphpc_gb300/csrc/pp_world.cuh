@@ -1,0 +1,102 @@
+/*
+ * pp_world.cuh -- host-side owner of one world: device buffers, the run
+ * table, the per-iteration launch sequence (captured as CUDA graphs) and
+ * the stats ring. A single simulation is a world of one run; batched and
+ * served runs share one world.
+ */
+#pragma once
+
+#include <vector>
+#include <cstring>
+
+#include "pp_kernels.cuh"
+
+namespace pp {
+
+struct RunSpec {
+	PPParameters p;
+	uint64_t seed;
+	uint32_t iters;          /* UINT32_MAX = open-ended */
+};
+
+struct WorldConfig {
+	int device = 0;
+	uint32_t tile_cells = 0;       /* 0 = choose */
+	uint32_t digit_bits = 0;       /* 0 = choose */
+	uint32_t cap = 0;              /* agent slots */
+	uint32_t ring_rows = 4096;
+	uint32_t graph_iters = 32;     /* iterations per captured graph, 0 = no graphs */
+	uint32_t nruns_cap = 0;        /* run slots (>= number of runs) */
+	uint32_t extra_tiles = 0;      /* free tile space for later admissions */
+	uint32_t act_cap = 0;          /* 0 = choose */
+	uint32_t max_cells_hint = 0;   /* largest run (cells), for serving worlds */
+};
+
+class World {
+public:
+	World() {}
+	~World();
+
+	/* Build the world for the given runs (each initialised at world
+	 * iteration 0). Returns a pp_error_codes value. */
+	int create(const std::vector<RunSpec> &runs, const WorldConfig &cfg);
+
+	/* Enqueue n iterations; no host synchronisation. */
+	int enqueue(uint32_t n);
+
+	/* Wait and check the device error flags. */
+	int sync_check();
+
+	/* Copy the stats rows of run r for world iterations [g0, g1] (ring
+	 * positions must still be valid). */
+	int read_rows(uint32_t r, uint32_t g0, uint32_t g1, PPStatistics *out);
+
+	/* Admission of a run into a free slot and tile range (serving). */
+	int admit(const RunSpec &spec, uint32_t *slot_out);
+	int retire(uint32_t slot);
+	bool fits(const RunSpec &spec) const;
+
+	uint32_t giter() const { return giter_; }
+	uint32_t nruns() const { return (uint32_t) runs_h_.size(); }
+	const RunDev &run(uint32_t r) const { return runs_h_[r]; }
+	uint32_t n_agents_dev();      /* reads the device counter (syncs) */
+	cudaStream_t stream() const { return s_; }
+	WorldDev &dev() { return w_; }
+	const LaunchCfg &launch() const { return lc_; }
+	size_t bytes() const { return bytes_; }
+	uint32_t ring_rows() const { return w_.ring_rows; }
+	uint32_t tile_cells() const { return 1u << w_.log_tile; }
+	int get_state(uint32_t *cell, uint32_t *en, uint32_t n_max,
+		uint32_t *n_out, uint16_t *grass, uint32_t r);
+
+private:
+	int alloc(size_t bytes, void **p);
+	int build_graph();
+	int init_run_device(uint32_t r, uint32_t base, const RunSpec &spec);
+	void free_all();
+
+	int device_ = 0;
+	cudaStream_t s_ = nullptr;
+	WorldDev w_{};
+	LaunchCfg lc_{};
+	std::vector<RunDev> runs_h_;
+	std::vector<uint16_t> tile_run_h_;
+	std::vector<void *> allocs_;
+	size_t bytes_ = 0;
+	uint32_t giter_ = 0;
+	uint32_t graph_iters_ = 0;
+	cudaGraphExec_t gexec_ = nullptr;
+	cudaGraph_t graph_ = nullptr;
+	uint32_t used_tiles_ = 0;
+	uint32_t null_slot_ = 0;
+	std::vector<std::pair<uint32_t, uint32_t>> free_tiles_; /* (first, count) */
+	uint32_t agents_reserved_ = 0;
+	std::vector<uint32_t> reserve_of_;
+};
+
+/* Pick tile size and digit width for a world. */
+void choose_geometry(uint32_t total_cells, uint32_t cap, WorldConfig &cfg);
+
+int cuda_status(cudaError_t e);
+
+} /* namespace pp */

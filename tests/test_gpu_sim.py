@@ -1,0 +1,103 @@
+"""Whole-step parity on the GPU: every stats row and the full agent/grass
+state, bit-exact against the oracle, for small grids and edge cases."""
+import numpy as np
+import pytest
+
+import pphpc_gb300 as pp
+from oracle import pp_oracle as orc
+from common import params, rows_array, first_diff
+
+pytestmark = pytest.mark.gpu
+
+
+def _check_run(p, seed, iters, **kw):
+    got = rows_array(pp.run(p, seed, iters, **kw))
+    want = orc.run(p, seed, iters)
+    d = first_diff(got, want)
+    assert d is None, d
+    return got
+
+
+@pytest.mark.parametrize("side,version,seed,iters", [
+    (25, 1, 0, 400), (25, 2, 1, 300), (50, 1, 2, 500), (50, 2, 3, 300),
+    (100, 1, 0, 1000), (64, 2, 9, 200), (33, 1, 17, 300)])
+def test_stats_bit_exact(side, version, seed, iters):
+    _check_run(params(side, version), seed, iters)
+
+
+@pytest.mark.parametrize("tile", [1024, 2048, 4096])
+def test_tile_sizes_agree(tile):
+    _check_run(params(70, 2), 5, 150, tile_cells=tile)
+
+
+@pytest.mark.parametrize("digit_bits", [5, 6, 8])
+def test_digit_widths_agree(digit_bits):
+    _check_run(params(60, 1), 4, 150, digit_bits=digit_bits)
+
+
+def test_without_graph():
+    _check_run(params(40, 1), 11, 100, use_graph=False)
+
+
+@pytest.mark.parametrize("gx,gy,s,w", [(1, 1, 5, 3), (1, 50, 20, 10), (50, 1, 20, 10),
+                                       (7, 13, 40, 20), (300, 2, 30, 30)])
+def test_degenerate_grids(gx, gy, s, w):
+    _check_run(params(0, 1, gx=gx, gy=gy, sheep=s, wolves=w), 3, 120)
+
+
+@pytest.mark.parametrize("s,w", [(0, 0), (50, 0), (0, 50)])
+def test_single_species_and_empty(s, w):
+    _check_run(params(30, 1, sheep=s, wolves=w), 8, 150)
+
+
+def test_crowded_cells():
+    # many agents per cell: exercises long in-cell orderings and the
+    # shared-memory overflow path of the act kernel
+    _check_run(params(0, 2, gx=20, gy=20, sheep=3000, wolves=1500), 12, 60,
+               max_agents=400_000)
+
+
+def test_state_bit_exact_after_steps():
+    p = params(40, 2)
+    seed = 21
+    o = orc.State(p, seed, capacity=1 << 20)
+    with pp.Simulation(p, seed, max_agents=1 << 20) as sim:
+        cell, en, grass = sim.state()
+        ocell, oen = o.agents()
+        assert np.array_equal(cell, ocell) and np.array_equal(en, oen)
+        assert np.array_equal(grass, o.grass())
+        for k in range(1, 40):
+            sim.step(1)
+            o.step()
+            cell, en, grass = sim.state()
+            ocell, oen = o.agents()
+            assert np.array_equal(cell, ocell), k
+            assert np.array_equal(en, oen), k
+            assert np.array_equal(grass, o.grass()), k
+
+
+def test_chunked_steps_equal_single_call():
+    p = params(30, 1)
+    a = rows_array(pp.run(p, 6, 300))
+    with pp.Simulation(p, 6) as sim:
+        rows = [sim.stats0()]
+        for n in (1, 7, 50, 100, 142):
+            rows += sim.step(n)
+    assert np.array_equal(a, rows_array(rows))
+
+
+def test_pool_overflow_reports_error():
+    p = params(50, 2)
+    with pytest.raises(pp.PPError) as ei:
+        pp.run(p, 1, 200, max_agents=1500)
+    assert ei.value.code == pp.PP_OUT_OF_RESOURCES
+
+
+def test_invariants_long_run():
+    p = params(100, 1)
+    rows = rows_array(pp.run(p, 0, 2000))
+    restart = p.grass_restart
+    cells = p.grid_x * p.grid_y
+    assert np.all(rows[:, 2] <= cells)
+    assert np.all(rows[:, 5] <= cells * restart)
+    assert np.all((rows[:, 0] == 0) | (rows[:, 3] >= rows[:, 0]))
