@@ -159,6 +159,36 @@ int pp_sim_info(pp_sim *sim, uint32_t *iter, uint32_t *n_agents,
 int pp_sim_get_state(pp_sim *sim, uint32_t *cell, uint32_t *en,
 	uint32_t n_max, uint32_t *n_agents, uint16_t *grass);
 
+/* Per-kernel timing (replaces the reference's cf4ocl event profiler,
+ * pp_gpu.c:1868-1881 and --prof-agg, pp_common.c:248-260): runs n_iters
+ * iterations without graph replay, with CUDA events on the simulation's
+ * stream around every kernel. prof[0..3] = move, radix_pass, offsets, act:
+ * launches, total milliseconds and algorithmic bytes moved (minimum reads
+ * plus writes of each kernel). `agent_steps` = sum of live agents at the
+ * start of each iteration. n_prof must be >= 4. */
+typedef struct pp_kernel_prof {
+	char name[32];
+	uint32_t launches;
+	double total_ms;
+	double bytes;
+} pp_kernel_prof;
+
+int pp_sim_profile(pp_sim *sim, uint32_t n_iters, pp_kernel_prof *prof,
+	uint32_t n_prof, double *agent_steps);
+
+/* Run n_iters iterations (graph replay) between two CUDA events on the
+ * simulation's stream; *ms = elapsed device time. */
+int pp_sim_time(pp_sim *sim, uint32_t n_iters, float *ms);
+
+/* Stats rows of iterations [first_iter, first_iter + n) still held in the
+ * device ring (the last ring_rows - 1 iterations). */
+int pp_sim_stats_range(pp_sim *sim, uint32_t first_iter, uint32_t n,
+	PPStatistics *out);
+
+/* Bytes the simulation has copied host->device and device->host so far
+ * (parameters, run tables, stats rows, status words). */
+int pp_sim_io_bytes(pp_sim *sim, uint64_t *h2d, uint64_t *d2h);
+
 /* The cudaStream_t the simulation runs on (as void*). */
 void *pp_sim_stream(pp_sim *sim);
 

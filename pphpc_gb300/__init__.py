@@ -98,6 +98,11 @@ class PPServeEvent(C.Structure):
                 ("n_rows", C.c_uint32), ("done", C.c_uint32)]
 
 
+class KernelProf(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint32),
+                ("total_ms", C.c_double), ("bytes", C.c_double)]
+
+
 STATS_CB = C.CFUNCTYPE(None, C.c_int, C.POINTER(PPStatistics), C.c_uint32,
                        C.c_void_p)
 
@@ -118,6 +123,12 @@ ABI = {
     "pp_sim_info": (C.c_int, [C.c_void_p, _u32p, _u32p, _u32p]),
     "pp_sim_get_state": (C.c_int, [C.c_void_p, _u32p, _u32p, C.c_uint32, _u32p, _P(C.c_uint16)]),
     "pp_sim_stream": (C.c_void_p, [C.c_void_p]),
+    "pp_sim_profile": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32,
+                                 _P(C.c_double)]),
+    "pp_sim_time": (C.c_int, [C.c_void_p, C.c_uint32, _P(C.c_float)]),
+    "pp_sim_stats_range": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32,
+                                     _P(PPStatistics)]),
+    "pp_sim_io_bytes": (C.c_int, [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)]),
     "pp_sim_destroy": (C.c_int, [C.c_void_p]),
     "pp_philox_fill": (C.c_int, [C.c_uint32] * 7 + [_u32p]),
     "pp_move_host": (C.c_int, [_P(PPParameters), C.c_uint64, C.c_uint32, C.c_uint32,
@@ -222,6 +233,35 @@ class Simulation:
         rows = (PPStatistics * max(n, 1))()
         _check(lib().pp_sim_step(self._h, n, rows), "pp_sim_step")
         return list(rows)[:n]
+
+    def time(self, n):
+        """Run n iterations between CUDA events on the simulation's
+        stream; returns the device time in milliseconds."""
+        ms = C.c_float()
+        _check(lib().pp_sim_time(self._h, n, C.byref(ms)), "pp_sim_time")
+        return ms.value
+
+    def stats_range(self, first_iter, n):
+        rows = (PPStatistics * max(n, 1))()
+        _check(lib().pp_sim_stats_range(self._h, first_iter, n, rows),
+               "pp_sim_stats_range")
+        return list(rows)[:n]
+
+    def profile(self, n):
+        """Per-kernel CUDA-event timing over n iterations: a list of
+        (name, launches, total_ms, algorithmic_bytes) and the agent-steps."""
+        prof = (KernelProf * 4)()
+        steps = C.c_double()
+        _check(lib().pp_sim_profile(self._h, n, prof, 4, C.byref(steps)),
+               "pp_sim_profile")
+        return ([(k.name.decode(), k.launches, k.total_ms, k.bytes) for k in prof],
+                steps.value)
+
+    def io_bytes(self):
+        h2d, d2h = C.c_uint64(), C.c_uint64()
+        _check(lib().pp_sim_io_bytes(self._h, C.byref(h2d), C.byref(d2h)),
+               "pp_sim_io_bytes")
+        return h2d.value, d2h.value
 
     def info(self):
         it, na, cap = C.c_uint32(), C.c_uint32(), C.c_uint32()

@@ -538,28 +538,35 @@ __global__ void k_philox_fill(uint32_t c0, uint32_t c1, uint32_t c2,
 /* ------------------------------------------------------------------ */
 
 cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
-	cudaStream_t s)
+	cudaStream_t s, const cudaEvent_t *marks)
 {
+	/* marks (optional, passes + 4 events): before the move, after the
+	 * move, after each radix pass, after the offsets, after the act. */
+	if (marks) cudaEventRecord(marks[0], s);
 	size_t hist_smem = (size_t) (w.passes << w.digit_bits) * sizeof(uint32_t);
 	k_move<<<lc.move_blocks, 256, hist_smem, s>>>(w);
+	if (marks) cudaEventRecord(marks[1], s);
 	uint32_t *ki = w.kB, *vi = w.vB, *ko = w.kC, *vo = w.vC;
 	for (uint32_t p = 0; p < w.passes; p++) {
 		cudaError_t e = launch_radix_pass(ki, vi, ko, vo, w.hist + p * 256,
 			w.lb_sort, w.ctr, &w.ctr->n_agents, p, p * w.digit_bits,
 			w.digit_bits, lc.sort_blocks, s);
 		if (e != cudaSuccess) return e;
+		if (marks) cudaEventRecord(marks[2 + p], s);
 		uint32_t *tk = ki, *tv = vi;
 		ki = ko; vi = vo; ko = tk; vo = tv;
 	}
 	/* ki/vi now hold the cell-sorted agents (dead ones last). */
 	k_offsets<<<lc.offs_blocks, 256, 0, s>>>(ki, &w.ctr->n_agents,
 		w.log_tile, w.n_tiles, w.tile_off);
+	if (marks) cudaEventRecord(marks[2 + w.passes], s);
 	size_t act_smem = (size_t) w.act_cap * 4 * sizeof(uint32_t);
 	switch (lc.cpt) {
 	case 4: k_act<4><<<lc.act_blocks, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
 	case 16: k_act<16><<<lc.act_blocks, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
 	default: k_act<8><<<lc.act_blocks, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
 	}
+	if (marks) cudaEventRecord(marks[3 + w.passes], s);
 	return cudaGetLastError();
 }
 

@@ -47,7 +47,7 @@ constexpr int ACT_THREADS = 256;
 /* One iteration: move, radix passes, tile offsets, act. Returns a CUDA
  * error code (cudaSuccess = 0). */
 cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
-	cudaStream_t s);
+	cudaStream_t s, const cudaEvent_t *marks = nullptr);
 
 /* Initialise run r: grass of its tiles, its initial agents at A[base..),
  * and accumulate its initial stats into ring row `row`. */

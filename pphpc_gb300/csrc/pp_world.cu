@@ -221,6 +221,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	WorldCounters c{};
 	c.n_agents = base;
 	PP_CK(cudaMemcpyAsync(w_.ctr, &c, sizeof(c), cudaMemcpyHostToDevice, s_));
+	h2d_ += nruns_cap * sizeof(RunDev) + tiles * 2 + nruns_cap * 4 + sizeof(c);
 
 	/* Launch geometry. */
 	lc_.sms = sms;
@@ -291,6 +292,7 @@ int World::sync_check()
 	PP_CK(cudaStreamSynchronize(s_));
 	uint32_t err = 0;
 	PP_CK(cudaMemcpy(&err, &w_.ctr->err, 4, cudaMemcpyDeviceToHost));
+	d2h_ += 4;
 	if (err & ERRF_TIMEOUT) return PP_ERR_TIMEOUT;
 	if (err & ERRF_OVERFLOW) return PP_OUT_OF_RESOURCES;
 	return PP_SUCCESS;
@@ -318,6 +320,7 @@ int World::read_rows(uint32_t r, uint32_t g0, uint32_t g1, PPStatistics *out)
 		PP_CK(cudaMemcpy2DAsync(out + (g - g0), sizeof(PPStatistics),
 			&w_.ring[(size_t) pos * w_.nruns_cap + r], pitch,
 			sizeof(PPStatistics), cnt, cudaMemcpyDeviceToHost, s_));
+		d2h_ += (uint64_t) cnt * sizeof(PPStatistics);
 		g += cnt;
 	}
 	PP_CK(cudaStreamSynchronize(s_));
@@ -346,6 +349,55 @@ int World::get_state(uint32_t *cell, uint32_t *en, uint32_t n_max,
 		for (uint32_t i = 0; i < m; i++) cell[i] -= cb;
 	}
 	return PP_SUCCESS;
+}
+
+int World::profile(uint32_t n, pp_kernel_prof *prof, double *agent_steps)
+{
+	PP_CK(cudaSetDevice(device_));
+	const uint32_t P = w_.passes;
+	std::vector<cudaEvent_t> ev(P + 4);
+	for (auto &e : ev) PP_CK(cudaEventCreate(&e));
+	static const char *names[4] = {"move", "radix_pass", "offsets", "act"};
+	for (int k = 0; k < 4; k++) {
+		memset(&prof[k], 0, sizeof(prof[k]));
+		snprintf(prof[k].name, sizeof(prof[k].name), "%s", names[k]);
+	}
+	uint64_t live_cells = 0;
+	for (uint32_t r = 0; r < null_slot_; r++)
+		if (runs_h_[r].active) live_cells += runs_h_[r].ncells;
+	double steps = 0;
+	int rc = PP_SUCCESS;
+	for (uint32_t it = 0; it < n && rc == PP_SUCCESS; it++) {
+		uint32_t n_before = 0, n_live = 0, n_after = 0;
+		PP_CK(cudaMemcpyAsync(&n_before, &w_.ctr->n_agents, 4, cudaMemcpyDeviceToHost, s_));
+		PP_CK(cudaStreamSynchronize(s_));
+		rc = cuda_status(enqueue_iteration(w_, lc_, s_, ev.data()));
+		if (rc) break;
+		PP_CK(cudaMemcpyAsync(&n_live, &w_.tile_off[w_.n_tiles], 4, cudaMemcpyDeviceToHost, s_));
+		PP_CK(cudaMemcpyAsync(&n_after, &w_.ctr->n_agents, 4, cudaMemcpyDeviceToHost, s_));
+		PP_CK(cudaStreamSynchronize(s_));
+		giter_++;
+		float ms;
+		PP_CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+		prof[0].launches++; prof[0].total_ms += ms;
+		prof[0].bytes += 16.0 * n_before;
+		for (uint32_t p = 0; p < P; p++) {
+			PP_CK(cudaEventElapsedTime(&ms, ev[1 + p], ev[2 + p]));
+			prof[1].launches++; prof[1].total_ms += ms;
+			prof[1].bytes += 16.0 * n_before;
+		}
+		PP_CK(cudaEventElapsedTime(&ms, ev[1 + P], ev[2 + P]));
+		prof[2].launches++; prof[2].total_ms += ms;
+		prof[2].bytes += 4.0 * n_before + 4.0 * (w_.n_tiles + 1);
+		PP_CK(cudaEventElapsedTime(&ms, ev[2 + P], ev[3 + P]));
+		prof[3].launches++; prof[3].total_ms += ms;
+		prof[3].bytes += 4.0 * live_cells + 8.0 * n_live + 8.0 * n_after;
+		steps += n_before;
+	}
+	for (auto &e : ev) cudaEventDestroy(e);
+	if (agent_steps) *agent_steps = steps;
+	if (rc) return rc;
+	return sync_check();
 }
 
 bool World::fits(const RunSpec &spec) const
@@ -398,6 +450,8 @@ int World::admit(const RunSpec &spec, uint32_t *slot_out)
 	if (rc) return rc;
 	uint32_t nn = n + n0;
 	PP_CK(cudaMemcpyAsync(&w_.ctr->n_agents, &nn, 4, cudaMemcpyHostToDevice, s_));
+	h2d_ += sizeof(RunDev) + need * 2 + 4 + 4;
+	d2h_ += 4;
 	*slot_out = slot;
 	return PP_SUCCESS;
 }
@@ -572,6 +626,53 @@ extern "C" int pp_sim_get_state(pp_sim *sim, uint32_t *cell, uint32_t *en,
 {
 	if (!sim) return PP_INVALID_ARGS;
 	return sim->world.get_state(cell, en, n_max, n_agents, grass, 0);
+}
+
+extern "C" int pp_sim_profile(pp_sim *sim, uint32_t n_iters,
+	pp_kernel_prof *prof, uint32_t n_prof, double *agent_steps)
+{
+	if (!sim || !prof || n_prof < 4) return PP_INVALID_ARGS;
+	if (n_iters >= sim->world.ring_rows()) return PP_INVALID_ARGS;
+	return sim->world.profile(n_iters, prof, agent_steps);
+}
+
+extern "C" int pp_sim_time(pp_sim *sim, uint32_t n_iters, float *ms)
+{
+	if (!sim || !ms) return PP_INVALID_ARGS;
+	if (n_iters >= sim->world.ring_rows()) return PP_INVALID_ARGS;
+	World &w = sim->world;
+	cudaEvent_t a, b;
+	PP_CK(cudaSetDevice(w.dev_index()));
+	PP_CK(cudaEventCreate(&a));
+	PP_CK(cudaEventCreate(&b));
+	PP_CK(cudaEventRecord(a, w.stream()));
+	int rc = w.enqueue(n_iters);
+	PP_CK(cudaEventRecord(b, w.stream()));
+	if (rc == PP_SUCCESS) rc = w.sync_check();
+	if (rc == PP_SUCCESS) PP_CK(cudaEventElapsedTime(ms, a, b));
+	cudaEventDestroy(a);
+	cudaEventDestroy(b);
+	return rc;
+}
+
+extern "C" int pp_sim_stats_range(pp_sim *sim, uint32_t first_iter,
+	uint32_t n, PPStatistics *out)
+{
+	if (!sim || !out) return PP_INVALID_ARGS;
+	World &w = sim->world;
+	uint32_t g = w.giter();
+	if (n == 0) return PP_SUCCESS;
+	if (first_iter + n - 1 > g || g - first_iter >= w.ring_rows())
+		return PP_INVALID_ARGS;
+	return w.read_rows(0, first_iter, first_iter + n - 1, out);
+}
+
+extern "C" int pp_sim_io_bytes(pp_sim *sim, uint64_t *h2d, uint64_t *d2h)
+{
+	if (!sim) return PP_INVALID_ARGS;
+	if (h2d) *h2d = sim->world.h2d_;
+	if (d2h) *d2h = sim->world.d2h_;
+	return PP_SUCCESS;
 }
 
 extern "C" void *pp_sim_stream(pp_sim *sim)

@@ -61,6 +61,7 @@ public:
 	const RunDev &run(uint32_t r) const { return runs_h_[r]; }
 	uint32_t n_agents_dev();      /* reads the device counter (syncs) */
 	cudaStream_t stream() const { return s_; }
+	int dev_index() const { return device_; }
 	WorldDev &dev() { return w_; }
 	const LaunchCfg &launch() const { return lc_; }
 	size_t bytes() const { return bytes_; }
@@ -68,6 +69,11 @@ public:
 	uint32_t tile_cells() const { return 1u << w_.log_tile; }
 	int get_state(uint32_t *cell, uint32_t *en, uint32_t n_max,
 		uint32_t *n_out, uint16_t *grass, uint32_t r);
+
+	/* Run n iterations without graphs, timing every kernel with CUDA
+	 * events on the world's stream; accumulates into prof[0..3] (move,
+	 * radix pass, offsets, act) with algorithmic bytes. */
+	int profile(uint32_t n, pp_kernel_prof *prof, double *agent_steps);
 
 private:
 	int alloc(size_t bytes, void **p);
@@ -91,6 +97,9 @@ private:
 	uint32_t null_slot_ = 0;
 	std::vector<std::pair<uint32_t, uint32_t>> free_tiles_; /* (first, count) */
 	uint32_t agents_reserved_ = 0;
+public:
+	uint64_t h2d_ = 0, d2h_ = 0;   /* bytes copied host<->device by the world */
+private:
 	std::vector<uint32_t> reserve_of_;
 };
 
