@@ -2,7 +2,8 @@
 
 Workload: plain PPHPC, 12800 x 12800 toroidal grid (163.84 M cells),
 parameter set v1 scaled by area (6,553,600 sheep, 3,276,800 wolves),
-seed 2, agent pool 4x the initial agents, uint32 SoA agents and uint16 grass.
+seed 2, agent pool 5x the initial agents (the v1 population peaks at 4.25x
+the initial agents near iteration 147), uint32 SoA agents, uint16 grass.
 A "step" is one simulation iteration over the whole grid.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -166,7 +167,7 @@ def run_ours(args, dist):
     dev = dist.local
     p = pp.make_params(**WORKLOAD)
     n0 = p.init_sheep + p.init_wolves
-    cap = 4 * n0
+    cap = 5 * n0
     K, W = args.steps, args.warmup
 
     # -- device-timed throughput (state resident in HBM) --

@@ -283,6 +283,7 @@ int World::enqueue(uint32_t n)
 	}
 	for (; done < n; done++) PP_CK(enqueue_iteration(w_, lc_, s_));
 	giter_ += n;
+	if (n) release_pending();
 	return PP_SUCCESS;
 }
 
@@ -469,7 +470,27 @@ int World::retire(uint32_t slot)
 	for (uint32_t t = 0; t < cnt; t++) tile_run_h_[first + t] = (uint16_t) null_slot_;
 	PP_CK(cudaMemcpyAsync(&w_.tile_run[first], &tile_run_h_[first], (size_t) cnt * 2,
 		cudaMemcpyHostToDevice, s_));
-	free_tiles_.push_back({first, cnt});
+	h2d_ += sizeof(RunDev) + (size_t) cnt * 2;
+	/* The run's last agents are still in the agent array; they die in the
+	 * next move (their tiles now map to the inactive null slot). Until an
+	 * iteration has run, the tiles must not be handed to another run. */
+	pending_tiles_.push_back({{first, cnt}, giter_});
+	return PP_SUCCESS;
+}
+
+void World::release_pending()
+{
+	bool any = false;
+	for (size_t i = 0; i < pending_tiles_.size();) {
+		if (pending_tiles_[i].second < giter_) {
+			free_tiles_.push_back(pending_tiles_[i].first);
+			pending_tiles_.erase(pending_tiles_.begin() + i);
+			any = true;
+		} else {
+			i++;
+		}
+	}
+	if (!any) return;
 	std::sort(free_tiles_.begin(), free_tiles_.end());
 	std::vector<std::pair<uint32_t, uint32_t>> merged;
 	for (auto &f : free_tiles_) {
@@ -478,7 +499,6 @@ int World::retire(uint32_t slot)
 		else merged.push_back(f);
 	}
 	free_tiles_.swap(merged);
-	return PP_SUCCESS;
 }
 
 } /* namespace pp */

@@ -96,6 +96,9 @@ private:
 	uint32_t used_tiles_ = 0;
 	uint32_t null_slot_ = 0;
 	std::vector<std::pair<uint32_t, uint32_t>> free_tiles_; /* (first, count) */
+	/* Tiles of retired runs, with the world iteration of retirement. */
+	std::vector<std::pair<std::pair<uint32_t, uint32_t>, uint32_t>> pending_tiles_;
+	void release_pending();
 	uint32_t agents_reserved_ = 0;
 public:
 	uint64_t h2d_ = 0, d2h_ = 0;   /* bytes copied host<->device by the world */

@@ -1,0 +1,178 @@
+"""The oracle (CPU checker) against the golden fixtures, against an
+independent pure-Python restatement of the reference's sequential in-cell
+semantics (pp_cpu.cl:640-848), and its invariants. No GPU needed."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pp_oracle as orc
+from common import params
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+FIELDS = ["init_sheep", "sheep_gain_from_food", "sheep_reproduce_threshold",
+          "sheep_reproduce_prob", "init_wolves", "wolves_gain_from_food",
+          "wolves_reproduce_threshold", "wolves_reproduce_prob", "grass_restart",
+          "grid_x", "grid_y", "iters"]
+TYPE = 0x80000000
+
+
+def test_philox_fixture():
+    ph = np.load(os.path.join(GOLDEN, "philox.npz"))
+    for i in range(3):
+        got = orc.philox_fill(tuple(int(x) for x in ph["ctr%d" % i]),
+                              tuple(int(x) for x in ph["key%d" % i]), 64)
+        assert np.array_equal(got, ph["out%d" % i])
+
+
+def test_philox_is_a_bijection_on_a_sample():
+    outs = orc.philox_fill((0, 0, 0, 0), (1, 2), 1 << 16)
+    assert len({tuple(r) for r in outs}) == 1 << 16
+
+
+def test_draw_range_and_uniformity():
+    w = orc.philox_fill((0, 1, 2, 0), (3, 4), 200_000)[:, 0]
+    for n in (1, 2, 5, 100, 12800):
+        d = (w.astype(np.uint64) * n) >> 32
+        assert d.max() < n
+        if n <= 100:
+            c = np.bincount(d.astype(np.int64), minlength=n)
+            assert c.min() > 0.9 * len(w) / n
+
+
+def test_golden_small_runs():
+    g = np.load(os.path.join(GOLDEN, "stats_small.npz"))
+    names = [k for k in g.files if not k.endswith(("_params", "_seed"))]
+    assert len(names) >= 7
+    for n in names:
+        d = dict(zip(FIELDS, (int(x) for x in g[n + "_params"])))
+        rows = orc.run(d, int(g[n + "_seed"][0]), len(g[n]) - 1)
+        assert np.array_equal(rows, g[n]), n
+
+
+def test_golden_100v1_full():
+    want = np.load(os.path.join(GOLDEN, "stats_100v1_s0.npz"))["rows"]
+    got = orc.run(params(100, 1, iters=4000), 0)
+    assert np.array_equal(got, want)
+
+
+def test_golden_400v2_prefix():
+    want = np.load(os.path.join(GOLDEN, "stats_400v2_s1.npz"))["rows"]
+    got = orc.run(params(400, 2, iters=200), 1)
+    assert np.array_equal(got, want[:201])
+
+
+def test_determinism_and_seed_sensitivity():
+    p = params(40, 2, iters=100)
+    a = orc.run(p, 5)
+    assert np.array_equal(a, orc.run(p, 5))
+    assert not np.array_equal(a, orc.run(p, 6))
+
+
+def test_invariants():
+    p = params(60, 2, iters=400)
+    rows = orc.run(p, 2)
+    cells = p.grid_x * p.grid_y
+    assert np.all(rows[:, 2] <= cells)
+    assert np.all(rows[:, 5] <= cells * p.grass_restart)
+    # every live agent has energy >= 1
+    assert np.all(rows[:, 3] >= rows[:, 0]) and np.all(rows[:, 4] >= rows[:, 1])
+
+
+def _seq_cell(order, types, energy, dice, grass, p):
+    """Sequential list semantics of pp_cpu.cl:640-848 for one cell whose
+    agents act in `order`: wolves eat the first sheep still in the list
+    (acted or not); a sheep removed before its turn does not act; the
+    acting sheep eats live grass; acting agents reproduce. Returns final
+    energies (0 = eaten), newborn energies and the grass."""
+    alive = {j: True for j in order}
+    lst = list(order)
+    en = dict(energy)
+    kid = {j: 0 for j in order}
+    for j in order:
+        if not alive[j]:
+            continue
+        if types[j] == 0:
+            if grass == 0:
+                grass = p["restart"]
+                en[j] += p["sgain"]
+            thr, prob = p["sthr"], p["sprob"]
+        else:
+            for k in lst:
+                if alive[k] and types[k] == 0:
+                    alive[k] = False
+                    en[j] += p["wgain"]
+                    break
+            thr, prob = p["wthr"], p["wprob"]
+        if en[j] > thr and dice[j] < prob:
+            kid[j] = en[j] // 2
+            en[j] -= kid[j]
+    fin = {j: (en[j] if alive[j] else 0) for j in order}
+    return fin, kid, grass
+
+
+@pytest.mark.parametrize("case", range(60))
+def test_act_closed_form_matches_sequential_lists(case):
+    rng = np.random.default_rng(case)
+    m = int(rng.integers(1, 13))
+    prob = int(rng.choice([0, 50, 100]))
+    p = params(5, 1)
+    p.sheep_reproduce_prob = prob
+    p.wolves_reproduce_prob = 100 - prob
+    p.sheep_reproduce_threshold = int(rng.integers(0, 6))
+    types = rng.integers(0, 2, m)
+    energy = rng.integers(1, 40, m)
+    cell = np.full(m, 7, np.uint32)
+    en = (energy | (types.astype(np.int64) << 31)).astype(np.uint32)
+    grass0 = np.zeros(p.grid_x * p.grid_y, np.uint16)
+    grass0[7] = int(rng.integers(0, 3))
+    seed, it = 11 + case, 3
+    co, eo, g = orc.act(p, seed, it, cell, en, grass0, 4 * m + 4)
+    # independent restatement with the same priorities and dice
+    pr = {}
+    dice = {}
+    for s in range(m):
+        w = orc.philox((s, it, 3, 0), (seed, 0))
+        pr[s] = w[0]
+        dice[s] = orc.draw(w[1], 100)
+    order = sorted(range(m), key=lambda s: (pr[s], s))
+    pp_ = dict(restart=p.grass_restart, sgain=p.sheep_gain_from_food,
+               wgain=p.wolves_gain_from_food, sthr=p.sheep_reproduce_threshold,
+               wthr=p.wolves_reproduce_threshold, sprob=p.sheep_reproduce_prob,
+               wprob=p.wolves_reproduce_prob)
+    fin, kid, gr = _seq_cell(order, {s: int(types[s]) for s in range(m)},
+                             {s: int(energy[s]) for s in range(m)}, dice, int(grass0[7]), pp_)
+    want = []
+    for s in range(m):
+        tb = int(types[s]) << 31
+        if fin[s]:
+            want.append(tb | fin[s])
+        if kid[s]:
+            want.append(tb | kid[s])
+    assert list(eo) == want
+    assert list(co) == [7] * len(want)
+    assert g[7] == gr
+
+
+def test_move_wraps_per_row():
+    p = params(4, 1, gx=4, gy=3)
+    cell = np.array([3, 0, 8, 11], np.uint32)
+    en = np.full(4, 10, np.uint32)
+    # find an iteration where each agent gets a given direction, check wrap
+    for it in range(1, 200):
+        c2, e2 = orc.move(p, 1, it, cell, en)
+        assert np.all(e2 == 9)
+        for i in range(4):
+            x, y = int(cell[i]) % 4, int(cell[i]) // 4
+            nx, ny = int(c2[i]) % 4, int(c2[i]) // 4
+            dx = (nx - x) % 4
+            dy = (ny - y) % 3
+            assert (dx, dy) in [(0, 0), (1, 0), (3, 0), (0, 1), (0, 2)]
+
+
+def test_pool_overflow():
+    p = params(50, 2, iters=200)
+    st = orc.State(p, 1, capacity=200)
+    with pytest.raises(RuntimeError):
+        for _ in range(200):
+            st.step()
