@@ -216,6 +216,27 @@ int pp_radix_sort_host(uint32_t n, const uint32_t *keys_in,
 	const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out,
 	uint32_t key_bits, uint32_t digit_bits);
 
+/* Largest n accepted by pp_radix_sort_noalloc. */
+#define PP_NOALLOC_SORT_MAX_N (1u << 22)
+
+/* No counterpart in the reference: it exists for callers that must not
+ * allocate device memory, such as an application whose device memory is
+ * owned by its own pooling allocator, or a loop with a latency budget in
+ * which cudaMalloc/cudaFree could synchronise the device. Same stable LSD
+ * radix sort as pp_radix_sort_host, but on caller-owned device buffers
+ * (`keys`, `vals` in; `keys_out`, `vals_out` out; the input buffers are
+ * overwritten as ping-pong space) and with its scratch in a fixed array
+ * inside the library (about 2 MB per GPU, held until the process exits).
+ * It calls no cudaMalloc/cudaFree. Limit: n <= PP_NOALLOC_SORT_MAX_N, else
+ * PP_INVALID_ARGS. The first call on a device looks up the array's device
+ * address; make that first call before any stream capture. All calls share
+ * the array: calls that overlap on the GPU (other streams, other threads)
+ * race and must be serialised by the caller. Runs on `stream` (a
+ * cudaStream_t, NULL = legacy stream) and returns after it completes. */
+int pp_radix_sort_noalloc(uint32_t n, uint32_t *keys, uint32_t *vals,
+	uint32_t *keys_out, uint32_t *vals_out, uint32_t key_bits,
+	uint32_t digit_bits, void *stream);
+
 /* Dense per-cell start offsets of a cell-sorted key array: off[c] = first
  * index with key >= c, for c = 0..n_cells (find_cell_idx,
  * pp_gpu.cl:834-867, as a full offset table). */

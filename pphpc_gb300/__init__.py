@@ -136,6 +136,8 @@ ABI = {
     "pp_radix_sort_host": (C.c_int, [C.c_uint32, _u32p, _u32p, _u32p, _u32p,
                                      C.c_uint32, C.c_uint32]),
     "pp_cell_offsets_host": (C.c_int, [C.c_uint32, _u32p, C.c_uint32, _u32p]),
+    "pp_radix_sort_noalloc": (C.c_int, [C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]),
     "pp_batch_opts_default": (None, [_P(PPBatchOpts)]),
     "pp_batch_run": (C.c_int, [_P(PPRunDesc), C.c_int, _P(PPBatchOpts), STATS_CB, C.c_void_p]),
     "pp_serve_opts_default": (None, [_P(PPServeOpts)]),
