@@ -162,10 +162,10 @@ int pp_sim_get_state(pp_sim *sim, uint32_t *cell, uint32_t *en,
 /* Per-kernel timing (replaces the reference's cf4ocl event profiler,
  * pp_gpu.c:1868-1881 and --prof-agg, pp_common.c:248-260): runs n_iters
  * iterations without graph replay, with CUDA events on the simulation's
- * stream around every kernel. prof[0..3] = move, radix_pass, offsets, act:
- * launches, total milliseconds and algorithmic bytes moved (minimum reads
- * plus writes of each kernel). `agent_steps` = sum of live agents at the
- * start of each iteration. n_prof must be >= 4. */
+ * stream around every kernel. prof[0..4] = move, radix_pass, offsets, act,
+ * finish: launches, total milliseconds and algorithmic bytes moved (minimum
+ * reads plus writes of each kernel). `agent_steps` = sum of live agents at
+ * the start of each iteration. n_prof must be >= 5. */
 typedef struct pp_kernel_prof {
 	char name[32];
 	uint32_t launches;

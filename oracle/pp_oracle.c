@@ -7,16 +7,22 @@
  * this file restates the model rules with Philox draws; see pp_oracle.h for
  * the reference lines each phase follows.
  *
- * Canonical step (iteration t = 1..iters), over an agent array in a defined
- * order and a grass countdown grid:
- *   1. move   -- slot i: energy <= 1 -> dies; else energy -= 1 and one of
- *               5 directions (stay, x+1, x-1, y+1, y-1, per-row toroidal
- *               wrap as in pp_gpu.cl:771-800) drawn from
- *               Philox(ctr={i, t, MOVE, 0}).w0.
+ * State: every cell holds an ordered list of agents; stored as an array
+ * stably sorted by cell (the initial agents are listed in creation order).
+ * Every draw is keyed by a cell and an agent's rank k in that cell's list,
+ * never by an array position, so any storage layout that keeps the lists
+ * gives the same results.
+ *
+ * Canonical step (iteration t = 1..iters):
+ *   1. move   -- agent of rank k in cell c: energy <= 1 -> dies; else
+ *               energy -= 1 and one of 5 directions (stay, x+1, x-1, y+1,
+ *               y-1, per-row toroidal wrap as in pp_gpu.cl:771-800) drawn
+ *               from Philox(ctr={c, t, MOVE, k}).w0.
  *   2. grass  -- countdown > 0 -> countdown - 1 (pp_gpu.cl:465).
- *   3. sort   -- stable sort of the survivors by cell index.
- *   4. act    -- per cell, agents in increasing (priority, slot) order,
- *               priority = Philox({s, t, ACT, 0}).w0 for sorted slot s.
+ *   3. sort   -- stable sort of the survivors by cell index: a cell's new
+ *               list is ordered by (source cell, rank in the source list).
+ *   4. act    -- per cell c, agents in increasing (priority, k) order,
+ *               priority = Philox({c, t, ACT, k}).w0 for new rank k.
  *               This is the sequential semantics of pp_cpu.cl:596-866
  *               with the shuffle replaced by the priority order:
  *               a wolf eats the first not-yet-eaten sheep of the cell
@@ -24,11 +30,11 @@
  *               yet eaten at its turn eats the grass if countdown == 0
  *               (countdown := restart, energy += gain); every agent that
  *               acts then reproduces if energy > threshold and
- *               draw(Philox({s, t, ACT, 0}).w1, 100) < prob: the child
+ *               draw(Philox({c, t, ACT, k}).w1, 100) < prob: the child
  *               gets energy/2 and the parent keeps the rest. Newborns
  *               neither act nor are eaten in their birth iteration.
- *               Output order: walk the sorted array; emit each surviving
- *               agent, then its newborn (if any).
+ *               Output (the cell's next list): its agents in rank order,
+ *               each surviving agent followed by its newborn (if any).
  *   5. stats  -- counts and energy sums over the output array; live grass
  *               (countdown == 0) and the countdown sum over the grid.
  */
@@ -72,9 +78,9 @@ uint32_t ppo_draw(uint32_t w, uint32_t n)
 }
 
 static void draw4(uint64_t seed, uint32_t id, uint32_t iter, uint32_t stream,
-	uint32_t out[4])
+	uint32_t k, uint32_t out[4])
 {
-	uint32_t ctr[4] = {id, iter, stream, 0};
+	uint32_t ctr[4] = {id, iter, stream, k};
 	uint32_t key[2] = {(uint32_t) seed, (uint32_t) (seed >> 32)};
 	ppo_philox(ctr, key, out);
 }
@@ -124,23 +130,26 @@ ppo_state *ppo_create(const ppo_params *p, uint64_t seed, uint32_t capacity)
 	/* Grass: alive (0) w.p. 1/2, else 1 + U[0, restart) (pp_gpu.cl:383-393). */
 	for (uint32_t c = 0; c < C; c++) {
 		uint32_t r[4];
-		draw4(seed, c, 0, PPO_STREAM_INIT_CELL, r);
+		draw4(seed, c, 0, PPO_STREAM_INIT_CELL, 0, r);
 		uint32_t alive = ppo_draw(r[0], 2);
 		s->grass[c] = alive ? 0
 			: (uint16_t) (1 + ppo_draw(r[1], p->grass_restart));
 	}
-	/* Agents: sheep first, then wolves (pp_gpu.cl:415-435). */
+	/* Agents: sheep first, then wolves (pp_gpu.cl:415-435); each cell's
+	 * list holds its agents in this creation order, i.e. the array is
+	 * stably sorted by cell. */
 	for (uint32_t a = 0; a < n0; a++) {
 		uint32_t r[4];
-		draw4(seed, a, 0, PPO_STREAM_INIT_AGENT, r);
+		draw4(seed, a, 0, PPO_STREAM_INIT_AGENT, 0, r);
 		uint32_t x = ppo_draw(r[0], p->grid_x);
 		uint32_t y = ppo_draw(r[1], p->grid_y);
 		uint32_t wolf = a >= p->init_sheep;
 		uint32_t gain = wolf ? p->wolves_gain : p->sheep_gain;
 		uint32_t e = 1 + ppo_draw(r[2], 2 * gain);
-		s->cell[a] = y * p->grid_x + x;
-		s->en[a] = (wolf ? PPO_TYPE_BIT : 0) | e;
+		s->cell2[a] = y * p->grid_x + x;
+		s->en2[a] = (wolf ? PPO_TYPE_BIT : 0) | e;
 	}
+	ppo_sort((uint32_t) n0, s->cell2, s->en2, s->cell, s->en, C);
 	s->n = (uint32_t) n0;
 	s->iter = 0;
 	return s;
@@ -178,16 +187,20 @@ void ppo_move(const ppo_params *p, uint64_t seed, uint32_t iter, uint32_t n,
 	uint32_t *cell_out, uint32_t *en_out)
 {
 	uint32_t GX = p->grid_x, GY = p->grid_y, C = p->grid_x * p->grid_y;
+	/* rank[c] = agents of cell c seen so far: an agent's rank is its
+	 * position in its cell's list (earlier array entries of that cell). */
+	uint32_t *rank = calloc((size_t) C + 1, sizeof(uint32_t));
 	for (uint32_t i = 0; i < n; i++) {
 		uint32_t en = en_in[i];
 		uint32_t e = energy_of(en);
+		uint32_t k = cell_in[i] < C ? rank[cell_in[i]]++ : 0;
 		if (e <= 1) {
 			cell_out[i] = C;           /* dead: sorts after every cell */
 			en_out[i] = en & PPO_TYPE_BIT;
 			continue;
 		}
 		uint32_t r[4];
-		draw4(seed, i, iter, PPO_STREAM_MOVE, r);
+		draw4(seed, cell_in[i], iter, PPO_STREAM_MOVE, k, r);
 		uint32_t dir = ppo_draw(r[0], 5);
 		uint32_t x = cell_in[i] % GX, y = cell_in[i] / GX;
 		switch (dir) {
@@ -200,6 +213,7 @@ void ppo_move(const ppo_params *p, uint64_t seed, uint32_t iter, uint32_t n,
 		cell_out[i] = y * GX + x;
 		en_out[i] = (en & PPO_TYPE_BIT) | (e - 1);
 	}
+	free(rank);
 }
 
 void ppo_sort(uint32_t n, const uint32_t *k_in, const uint32_t *v_in,
@@ -250,7 +264,7 @@ int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
 		uint32_t m = hi - lo, S = 0, W = 0;
 		for (uint32_t j = 0; j < m; j++) {
 			uint32_t s = lo + j, r[4];
-			draw4(seed, s, iter, PPO_STREAM_ACT, r);
+			draw4(seed, c, iter, PPO_STREAM_ACT, j, r);
 			ord[j].prio = r[0];
 			ord[j].slot = s;
 			dice[s] = ppo_draw(r[1], 100);

@@ -82,7 +82,8 @@ void ppo_get_agents(const ppo_state *s, uint32_t *cell, uint32_t *en);
 void ppo_get_grass(const ppo_state *s, uint16_t *grass);
 
 /* Phase functions over caller arrays (for kernel-level checks). */
-/* Move of iteration `iter`: dead agents get cell = grid_xy. */
+/* Move of iteration `iter`: dead agents get cell = grid_xy. An agent's
+ * draw uses its cell and its rank among the earlier entries of that cell. */
 void ppo_move(const ppo_params *p, uint64_t seed, uint32_t iter, uint32_t n,
 	const uint32_t *cell_in, const uint32_t *en_in,
 	uint32_t *cell_out, uint32_t *en_out);

@@ -252,9 +252,9 @@ class Simulation:
     def profile(self, n):
         """Per-kernel CUDA-event timing over n iterations: a list of
         (name, launches, total_ms, algorithmic_bytes) and the agent-steps."""
-        prof = (KernelProf * 4)()
+        prof = (KernelProf * 5)()
         steps = C.c_double()
-        _check(lib().pp_sim_profile(self._h, n, prof, 4, C.byref(steps)),
+        _check(lib().pp_sim_profile(self._h, n, prof, 5, C.byref(steps)),
                "pp_sim_profile")
         return ([(k.name.decode(), k.launches, k.total_ms, k.bytes) for k in prof],
                 steps.value)

@@ -74,10 +74,12 @@ __host__ __device__ __forceinline__ uint32_t draw(uint32_t w, uint32_t n)
 #endif
 }
 
+/* The draw of (cell or agent number `id`, iteration, stream, rank k in the
+ * cell's list) under the run's seed. */
 __host__ __device__ __forceinline__ u4 rng(uint32_t seed_lo, uint32_t seed_hi,
-	uint32_t id, uint32_t iter, uint32_t stream)
+	uint32_t id, uint32_t iter, uint32_t stream, uint32_t k)
 {
-	return philox4x32_10(u4{id, iter, stream, 0u}, seed_lo, seed_hi);
+	return philox4x32_10(u4{id, iter, stream, k}, seed_lo, seed_hi);
 }
 
 /* Unsigned division by a runtime constant d >= 1 via a precomputed
@@ -137,9 +139,9 @@ struct WorldCounters {
 	uint32_t seq;            /* look-back epoch base, +1 per iteration   */
 	uint32_t err;            /* ERRF_* bits                              */
 	uint32_t act_ticket;     /* act tile tickets                          */
-	uint32_t act_done;       /* act CTAs finished                         */
+	uint32_t finish_done;    /* finish CTAs done                          */
 	uint32_t sort_ticket[8]; /* one per radix pass                        */
-	uint32_t move_done;
+	uint32_t aux_n;          /* element count of a standalone sort        */
 	uint32_t pad[3];
 };
 

@@ -8,18 +8,19 @@
  *                 bucket (a tile of cells, or a single cell) in the
  *                 cell-sorted agent array.
  *   k_act         grass (pp_gpu.cl:448-476) + action_agent
- *                 (pp_gpu.cl:883-979) + reduce_grass1/2 and
- *                 reduce_agent1/2 (pp_gpu.cl:485-736), fused per tile of
- *                 cells: countdown, in-cell conflict resolution in priority
- *                 order, newborn slots by a block prefix sum, compaction of
- *                 survivors and newborns with a decoupled look-back across
- *                 tiles, and the stats (warp shuffles, one atomic per
- *                 field per block and run).
+ *                 (pp_gpu.cl:883-979), fused per tile of cells: countdown,
+ *                 in-cell conflict resolution in priority order, newborn
+ *                 slots by a block prefix sum, compaction of survivors and
+ *                 newborns with a warp-wide decoupled look-back across
+ *                 tiles, and per-tile partial stats.
+ *   k_finish      reduce_grass1/2 + reduce_agent1/2 (pp_gpu.cl:485-736):
+ *                 the per-tile partial stats summed per run into the stats
+ *                 ring; its last CTA advances the iteration.
  *   k_init_*      init_cell / init_agent (pp_gpu.cl:368-439).
  *
- * Every kernel is grid-stride or ticket-persistent and reads its sizes
- * from device memory, so one iteration is a fixed launch sequence that is
- * captured once as a CUDA graph.
+ * Draws are keyed by (cell, rank of the agent in its cell's list), never by
+ * an array position. Every kernel reads its sizes from device memory, so an
+ * iteration is a fixed launch sequence, captured once as a CUDA graph.
  */
 #include "pp_kernels.cuh"
 #include "pp_block.cuh"
@@ -30,10 +31,10 @@ namespace pp {
 /* Move                                                                */
 /* ------------------------------------------------------------------ */
 
-/* Energy loss, death and toroidal random walk of one agent
- * (pp_gpu.cl:756-819; per-row wrap as there). */
+/* Energy loss, death and toroidal random walk of one agent of rank k in
+ * its cell (pp_gpu.cl:756-819; per-row wrap as there). */
 __device__ __forceinline__ void move_one(const RunDev &run, uint32_t key,
-	uint32_t val, uint32_t id, uint32_t t, uint32_t dead_key,
+	uint32_t val, uint32_t k, uint32_t t, uint32_t dead_key,
 	uint32_t &nk, uint32_t &nv)
 {
 	uint32_t e = val & ENERGY_MASK;
@@ -42,9 +43,9 @@ __device__ __forceinline__ void move_one(const RunDev &run, uint32_t key,
 		nv = val & TYPE_BIT;
 		return;
 	}
-	u4 r = rng(run.seed_lo, run.seed_hi, id, t, STREAM_MOVE);
-	uint32_t dir = draw(r.x, 5);
 	uint32_t lc = key - run.cbase;
+	u4 r = rng(run.seed_lo, run.seed_hi, lc, t, STREAM_MOVE, k);
+	uint32_t dir = draw(r.x, 5);
 	uint32_t y = fastdiv_div(lc, run.gxdiv);
 	uint32_t x = lc - y * run.gx;
 	if (dir == 1) x = (x + 1 == run.gx) ? 0 : x + 1;
@@ -60,6 +61,27 @@ __device__ __forceinline__ bool run_live(const RunDev &run, uint32_t t)
 	return run.active && t >= 1 && t <= run.iters;
 }
 
+/* Rank of each lane's agent in its cell's list, for a warp holding the
+ * consecutive, cell-sorted slots base .. base + 31 of `keys` (lanes past
+ * n hold invalid slots). Lane 0 counts the run of equal keys before the
+ * warp; the rest follows from a ballot of run starts. */
+__device__ __forceinline__ uint32_t warp_cell_rank(const uint32_t *keys,
+	uint32_t i, uint32_t key, bool valid, uint32_t lane)
+{
+	uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+	bool start = (lane == 0) ? true : (key != prev);
+	uint32_t starts = __ballot_sync(0xffffffffu, start && valid);
+	uint32_t r0 = 0;
+	if (lane == 0 && valid) {
+		uint32_t j = i;
+		while (j > 0 && keys[j - 1] == key) { j--; r0++; }
+	}
+	r0 = __shfl_sync(0xffffffffu, r0, 0);
+	uint32_t upto = starts & (0xffffffffu >> (31 - lane));
+	uint32_t s = 31 - __clz(upto);   /* last run start at or before lane */
+	return s == 0 ? r0 + lane : lane - s;
+}
+
 __global__ void __launch_bounds__(256) k_move(WorldDev w)
 {
 	extern __shared__ uint32_t sh_hist[];
@@ -72,17 +94,18 @@ __global__ void __launch_bounds__(256) k_move(WorldDev w)
 	const uint32_t lane = threadIdx.x & 31;
 	const uint32_t stride = gridDim.x * blockDim.x;
 	for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-		uint32_t i = base + threadIdx.x;
-		bool valid = i < n;
-		uint32_t nk = 0xffffffffu, nv;
+		const uint32_t i = base + threadIdx.x;
+		const bool valid = i < n;
+		uint32_t key = valid ? w.kA[i] : 0xffffffffu;
+		uint32_t val = valid ? w.vA[i] : 0;
+		uint32_t k = warp_cell_rank(w.kA, i, key, valid, lane);
+		uint32_t nk = 0xffffffffu, nv = 0;
 		if (valid) {
-			uint32_t key = w.kA[i], val = w.vA[i];
 			uint32_t r = w.tile_run[key >> w.log_tile];
 			const RunDev &run = w.runs[r];
 			uint32_t t = g - run.start_giter;
 			if (run_live(run, t)) {
-				move_one(run, key, val, i - w.run_base[r], t, w.dead_key,
-					nk, nv);
+				move_one(run, key, val, k, t, w.dead_key, nk, nv);
 			} else {
 				nk = w.dead_key;
 				nv = val & TYPE_BIT;
@@ -90,13 +113,19 @@ __global__ void __launch_bounds__(256) k_move(WorldDev w)
 			w.kB[i] = nk;
 			w.vB[i] = nv;
 		}
-		/* Warp-aggregated digit counts: the array is nearly cell-sorted,
-		 * so the high digits of a warp mostly coincide. */
+		/* Digit counts: one atomic per warp when the warp's digits agree
+		 * (the high digits of a nearly cell-sorted array), else one per
+		 * lane. */
 		for (uint32_t p = 0; p < P; p++) {
-			uint32_t dig = valid ? ((nk >> (p * d)) & mask) : 0xffffffffu;
-			uint32_t peers = __match_any_sync(0xffffffffu, dig);
-			if (valid && lane == (uint32_t) (__ffs(peers) - 1))
-				atomicAdd(&sh_hist[(p << d) + dig], __popc(peers));
+			uint32_t dig = (nk >> (p * d)) & mask;
+			uint32_t d0 = __shfl_sync(0xffffffffu, dig, 0);
+			uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+			bool same = __all_sync(0xffffffffu, !valid || dig == d0);
+			if (same) {
+				if (lane == 0 && vmask) atomicAdd(&sh_hist[(p << d) + d0], __popc(vmask));
+			} else if (valid) {
+				atomicAdd(&sh_hist[(p << d) + dig], 1u);
+			}
 		}
 	}
 	__syncthreads();
@@ -106,7 +135,7 @@ __global__ void __launch_bounds__(256) k_move(WorldDev w)
 	}
 }
 
-/* Move of one run alone (kernel-level check): slot i has id i. */
+/* Move of one run alone (kernel-level check) over a cell-sorted array. */
 __global__ void k_move_only(const uint32_t *kin, const uint32_t *vin,
 	uint32_t *kout, uint32_t *vout, uint32_t n, const RunDev *run_dev,
 	uint32_t t, uint32_t dead_key)
@@ -114,8 +143,10 @@ __global__ void k_move_only(const uint32_t *kin, const uint32_t *vin,
 	const RunDev run = *run_dev;
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
 		i += gridDim.x * blockDim.x) {
+		uint32_t k = 0;
+		while (k < i && kin[i - k - 1] == kin[i]) k++;
 		uint32_t nk, nv;
-		move_one(run, kin[i], vin[i], i, t, dead_key, nk, nv);
+		move_one(run, kin[i], vin[i], k, t, dead_key, nk, nv);
 		kout[i] = nk;
 		vout[i] = nv;
 	}
@@ -152,21 +183,26 @@ __global__ void k_offsets(const uint32_t *keys, const uint32_t *n_dev,
 /* Act                                                                 */
 /* ------------------------------------------------------------------ */
 
-/* Actions of the agents of one cell, slots [p, e) of the tile's agent
- * list, in increasing (priority, slot) order. This is the sequential
- * semantics of pp_cpu.cl:640-848 (wolves eat the first not-yet-eaten
- * sheep of the cell; a sheep acts only if not eaten before its turn; the
- * first acting sheep takes live grass; every acting agent may reproduce)
- * in closed form: the k-th wolf eats the k-th sheep, and a sheep acts iff
- * the wolves before it are no more than the sheep before it.
+/* Actions of the agents of one cell (local index lc), entries [p, e) of
+ * the tile's agent list in cell-list order, in increasing (priority, rank)
+ * order; priority and dice of the agent of rank k come from
+ * Philox({lc, t, ACT, k}). This is the sequential semantics of
+ * pp_cpu.cl:640-848 (wolves eat the first not-yet-eaten sheep of the cell;
+ * a sheep acts only if not eaten before its turn; the first acting sheep
+ * takes live grass; every acting agent may reproduce) in closed form: the
+ * k-th wolf eats the k-th sheep, and a sheep acts iff the wolves before it
+ * are no more than the sheep before it.
  * On return LV[j] holds type | final energy (energy 0 = eaten) and LD[j]
- * the newborn's energy (0 = none); on entry LD[j] holds the dice. */
+ * the newborn's energy (0 = none). */
 __device__ __forceinline__ void act_cell(uint32_t p, uint32_t e,
-	uint32_t *LV, const uint32_t *LP, uint32_t *LD, const RunDev &run,
-	uint32_t &g)
+	uint32_t *LV, uint32_t *LP, uint32_t *LD, const RunDev &run,
+	uint32_t lc, uint32_t t, uint32_t &g)
 {
 	uint32_t S = 0, W = 0;
 	for (uint32_t j = p; j < e; j++) {
+		u4 r = rng(run.seed_lo, run.seed_hi, lc, t, STREAM_ACT, j - p);
+		LP[j] = r.x;
+		LD[j] = draw(r.y, 100);
 		if (LV[j] & TYPE_BIT) W++;
 		else S++;
 	}
@@ -237,15 +273,69 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *a,
 	return lo;
 }
 
+/* Warp-wide decoupled look-back (lanes read 32 predecessors at once).
+ * Called by all lanes of one warp; returns the exclusive prefix of `tile`
+ * and publishes its inclusive prefix. Bounded: a predecessor that does not
+ * publish within SPIN_LIMIT polls raises ERRF_TIMEOUT. */
+__device__ uint32_t warp_lookback(uint64_t *lb, uint32_t tile, uint32_t agg,
+	uint32_t epoch, uint32_t *err)
+{
+	const uint32_t lane = threadIdx.x & 31;
+	if (tile == 0) {
+		if (lane == 0) st_release_u64(&lb[0], lb_pack(epoch, LB_FLAG_PREFIX, agg));
+		return 0;
+	}
+	if (lane == 0) st_release_u64(&lb[tile], lb_pack(epoch, LB_FLAG_AGG, agg));
+	const uint32_t ep = epoch & 0x3fffffffu;
+	uint32_t acc = 0;
+	int64_t end = (int64_t) tile;     /* window covers end-32 .. end-1 */
+	uint32_t spins = 0;
+	bool timed_out = false;
+	while (end > 0) {
+		int64_t idx = end - 1 - (int64_t) lane;
+		uint32_t flag, val;
+		for (;;) {
+			if (idx >= 0) {
+				uint64_t word = ld_acquire_u64(&lb[idx]);
+				bool cur = (uint32_t) (word >> 34) == ep;
+				flag = cur ? ((uint32_t) (word >> 32) & 3u) : 0u;
+				val = (uint32_t) word;
+			} else {
+				flag = (uint32_t) LB_FLAG_PREFIX;  /* before tile 0 */
+				val = 0;
+			}
+			if (__all_sync(0xffffffffu, flag != 0)) break;
+			if (++spins > SPIN_LIMIT) { timed_out = true; break; }
+			if (spins > 32) __nanosleep(64);
+		}
+		if (timed_out) {
+			if (lane == 0) atomicOr(err, ERRF_TIMEOUT);
+			break;
+		}
+		uint32_t pm = __ballot_sync(0xffffffffu, flag == LB_FLAG_PREFIX);
+		if (pm) {
+			uint32_t first = __ffs(pm) - 1;      /* nearest inclusive prefix */
+			uint32_t v = lane <= first ? val : 0;
+			acc += warp_sum(v);
+			break;
+		}
+		acc += warp_sum(val);
+		end -= 32;
+	}
+	if (lane == 0)
+		st_release_u64(&lb[tile], lb_pack(epoch, LB_FLAG_PREFIX, acc + agg));
+	return acc;
+}
+
 struct StatAcc {
 	uint32_t sheep, wolves, galive;
 	uint64_t sen, wen, gen;
 	__device__ void zero() { sheep = wolves = galive = 0; sen = wen = gen = 0; }
 };
 
-/* Block-reduce the per-thread stats and add them to the run's stats row
- * with one atomic per field. Must be called by all threads of the block. */
-__device__ void flush_stats(StatAcc &a, PPStatistics *dst)
+/* Block-reduce the per-thread stats into out[0..5] (u64, thread f writes
+ * field f). Must be called by all threads of the block. */
+__device__ void block_stats(const StatAcc &a, uint64_t *out)
 {
 	__shared__ uint64_t red[6][ACT_THREADS / 32];
 	uint64_t v[6] = {a.sheep, a.wolves, a.galive, a.sen, a.wen, a.gen};
@@ -259,21 +349,60 @@ __device__ void flush_stats(StatAcc &a, PPStatistics *dst)
 	if (threadIdx.x < 6) {
 		uint64_t s = 0;
 		for (uint32_t q = 0; q < ACT_THREADS / 32; q++) s += red[threadIdx.x][q];
-		if (s) {
-			switch (threadIdx.x) {
-			case 0: atomicAdd(&dst->sheep, (uint32_t) s); break;
-			case 1: atomicAdd(&dst->wolves, (uint32_t) s); break;
-			case 2: atomicAdd(&dst->grass, (uint32_t) s); break;
-			case 3: atomicAdd((unsigned long long *) &dst->sheep_en, s); break;
-			case 4: atomicAdd((unsigned long long *) &dst->wolves_en, s); break;
-			default: atomicAdd((unsigned long long *) &dst->grass_en, s); break;
-			}
-		}
+		out[threadIdx.x] = s;
 	}
 	__syncthreads();
-	a.zero();
 }
 
+__device__ __forceinline__ void stats_atomic_add(PPStatistics *dst,
+	uint32_t f, uint64_t s)
+{
+	if (!s) return;
+	switch (f) {
+	case 0: atomicAdd(&dst->sheep, (uint32_t) s); break;
+	case 1: atomicAdd(&dst->wolves, (uint32_t) s); break;
+	case 2: atomicAdd(&dst->grass, (uint32_t) s); break;
+	case 3: atomicAdd((unsigned long long *) &dst->sheep_en, s); break;
+	case 4: atomicAdd((unsigned long long *) &dst->wolves_en, s); break;
+	default: atomicAdd((unsigned long long *) &dst->grass_en, s); break;
+	}
+}
+
+template <int CPT>
+__device__ __forceinline__ void load_grass(const uint16_t *gp, uint16_t *gr)
+{
+	if (CPT == 4) {
+		uint2 q = *reinterpret_cast<const uint2 *>(gp);
+		memcpy(gr, &q, 8);
+	} else {
+#pragma unroll
+		for (int q = 0; q < CPT; q += 8) {
+			uint4 v = *reinterpret_cast<const uint4 *>(gp + q);
+			memcpy(gr + q, &v, 16);
+		}
+	}
+}
+
+template <int CPT>
+__device__ __forceinline__ void store_grass(uint16_t *gp, const uint16_t *gr)
+{
+	if (CPT == 4) {
+		uint2 q;
+		memcpy(&q, gr, 8);
+		*reinterpret_cast<uint2 *>(gp) = q;
+	} else {
+#pragma unroll
+		for (int q = 0; q < CPT; q += 8) {
+			uint4 v;
+			memcpy(&v, gr + q, 16);
+			*reinterpret_cast<uint4 *>(gp + q) = v;
+		}
+	}
+}
+
+/* One CTA per tile of CPT * 256 cells; tiles are taken by ticket so a
+ * tile's predecessors are always running or done (the look-back cannot
+ * wait on a CTA that is not resident). */
 template <int CPT>
 __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	const uint32_t *__restrict__ kS, uint32_t *__restrict__ vS)
@@ -281,189 +410,189 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	extern __shared__ uint32_t sm[];
 	uint32_t *sk = sm, *sv = sm + w.act_cap, *sp = sv + w.act_cap,
 		*sd = sp + w.act_cap;
-	__shared__ uint32_t s_tile, s_base, s_last;
+	__shared__ uint32_t s_tile, s_base;
+	__shared__ uint64_t s_part[6];
 	const uint32_t tid = threadIdx.x;
-	const uint32_t giter = w.ctr->giter;
-	const uint32_t g = giter + 1;
+	if (tid == 0) s_tile = atomicAdd(&w.ctr->act_ticket, 1u);
+	__syncthreads();
+	const uint32_t tile = s_tile;
+	if (tile >= w.n_tiles) return;
+	const uint32_t g = w.ctr->giter + 1;
 	const uint32_t epoch = w.ctr->seq * 8u + 7u;
-	const uint32_t row = g % w.ring_rows;
+	const uint32_t r = w.tile_run[tile];
+	const RunDev run = w.runs[r];
+	const uint32_t t = g - run.start_giter;
+	const bool live = run_live(run, t);
+	const uint32_t c0 = tile << w.log_tile;
+	const uint32_t cell0 = tid * CPT;
+	uint16_t gr[CPT];
+	uint16_t *gp = w.grass + c0 + cell0;
+	load_grass<CPT>(gp, gr);
+	const uint32_t a0 = w.tile_off[tile], a1 = w.tile_off[tile + 1];
+	const uint32_t m = a1 - a0;
+	const bool in_smem = m <= w.act_cap;
+	uint32_t *LK, *LV, *LP, *LD;
+	if (in_smem) {
+		LK = sk; LV = sv; LP = sp; LD = sd;
+		for (uint32_t j = tid; j < m; j += ACT_THREADS) {
+			sk[j] = kS[a0 + j];
+			sv[j] = vS[a0 + j];
+		}
+	} else {
+		LK = const_cast<uint32_t *>(kS) + a0;
+		LV = vS + a0;
+		LP = w.scratch_prio + a0;
+		LD = w.scratch_kid + a0;
+	}
+	__syncthreads();
 	StatAcc acc;
 	acc.zero();
-	int cur_run = -1;
-
-	for (;;) {
-		if (tid == 0) s_tile = atomicAdd(&w.ctr->act_ticket, 1u);
-		__syncthreads();
-		const uint32_t tile = s_tile;
-		if (tile >= w.n_tiles) break;
-		const uint32_t r = w.tile_run[tile];
-		if ((int) r != cur_run) {
-			if (cur_run >= 0)
-				flush_stats(acc, &w.ring[(size_t) row * w.nruns_cap + cur_run]);
-			cur_run = (int) r;
-		}
-		const RunDev run = w.runs[r];
-		const uint32_t t = g - run.start_giter;
-		const bool live = run_live(run, t);
-		const uint32_t c0 = tile << w.log_tile;
-		const uint32_t a0 = w.tile_off[tile], a1 = w.tile_off[tile + 1];
-		const uint32_t m = a1 - a0;
-		const uint32_t sbase = w.tile_off[run.first_tile];
-		const bool in_smem = m <= w.act_cap;
-		uint32_t *LK, *LV, *LP, *LD;
-		if (in_smem) {
-			LK = sk; LV = sv; LP = sp; LD = sd;
-		} else {
-			LK = const_cast<uint32_t *>(kS) + a0;
-			LV = vS + a0;
-			LP = w.scratch_prio + a0;
-			LD = w.scratch_kid + a0;
-		}
-		for (uint32_t j = tid; j < m; j += ACT_THREADS) {
-			uint32_t k = kS[a0 + j], v = vS[a0 + j];
-			if (in_smem) {
-				sk[j] = k;
-				sv[j] = v;
-			}
-			u4 rr = rng(run.seed_lo, run.seed_hi, a0 + j - sbase, t,
-				STREAM_ACT);
-			LP[j] = rr.x;
-			LD[j] = draw(rr.y, 100);
-		}
-		/* Grass of this thread's CPT cells (vector load). */
-		const uint32_t cell0 = tid * CPT;
-		uint16_t gr[CPT];
-		uint16_t *gp = w.grass + c0 + cell0;
-		if (CPT == 8) {
-			uint4 q = *reinterpret_cast<const uint4 *>(gp);
-			memcpy(gr, &q, 16);
-		} else if (CPT == 4) {
-			uint2 q = *reinterpret_cast<const uint2 *>(gp);
-			memcpy(gr, &q, 8);
-		} else {
+	const uint32_t lc0 = c0 - run.cbase + cell0;
+	const uint32_t pbeg = lower_bound_u32(LK, m, c0 + cell0);
+	const uint32_t pend = lower_bound_u32(LK, m, c0 + cell0 + CPT);
+	uint32_t p = pbeg;
 #pragma unroll
-			for (int q = 0; q < CPT; q += 8) {
-				uint4 v = *reinterpret_cast<const uint4 *>(gp + q);
-				memcpy(gr + q, &v, 16);
-			}
-		}
-		__syncthreads();
-		const uint32_t lc0 = c0 - run.cbase + cell0;
-		const uint32_t pbeg = lower_bound_u32(LK, m, c0 + cell0);
-		const uint32_t pend = lower_bound_u32(LK, m, c0 + cell0 + CPT);
-		uint32_t p = pbeg;
-#pragma unroll
-		for (int q = 0; q < CPT; q++) {
-			const uint32_t cell = c0 + cell0 + q;
-			const bool real = live && (lc0 + q) < run.ncells;
-			uint32_t gq = gr[q];
-			if (real && gq > 0) gq--;
-			uint32_t e = p;
-			while (e < pend && LK[e] == cell) e++;
-			if (e > p) {
-				if (real) {
-					act_cell(p, e, LV, LP, LD, run, gq);
-				} else {
-					for (uint32_t j = p; j < e; j++) {
-						LV[j] &= TYPE_BIT;
-						LD[j] = 0;
-					}
-				}
-			}
+	for (int q = 0; q < CPT; q++) {
+		const uint32_t cell = c0 + cell0 + q;
+		const bool real = live && (lc0 + q) < run.ncells;
+		uint32_t gq = gr[q];
+		if (real && gq > 0) gq--;
+		uint32_t e = p;
+		while (e < pend && LK[e] == cell) e++;
+		if (e > p) {
 			if (real) {
-				acc.galive += gq == 0;
-				acc.gen += gq;
-			}
-			gr[q] = (uint16_t) gq;
-			p = e;
-		}
-		/* Survivors + newborns of this thread, in slot order. */
-		uint32_t cnt = 0;
-		for (uint32_t j = pbeg; j < pend; j++)
-			cnt += ((LV[j] & ENERGY_MASK) != 0) + (LD[j] != 0);
-		uint32_t total;
-		const uint32_t excl = block_excl_scan(cnt, &total);
-		if (tid == 0) {
-			uint32_t base = lookback(w.lb_act, 1, tile, total, epoch,
-				&w.ctr->err);
-			s_base = base;
-			if (tile == run.first_tile) w.run_base[r] = base;
-			if (tile == w.n_tiles - 1)
-				w.ctr->n_agents = min(base + total, w.cap);
-		}
-		__syncthreads();
-		uint32_t o = s_base + excl;
-		for (uint32_t j = pbeg; j < pend; j++) {
-			const uint32_t v = LV[j], k = LK[j], kd = LD[j];
-			const uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
-			if (en) {
-				if (o < w.cap) {
-					w.kA[o] = k;
-					w.vA[o] = v;
-				}
-				o++;
-				if (tb) { acc.wolves++; acc.wen += en; }
-				else { acc.sheep++; acc.sen += en; }
-			}
-			if (kd) {
-				if (o < w.cap) {
-					w.kA[o] = k;
-					w.vA[o] = tb | kd;
-				}
-				o++;
-				if (tb) { acc.wolves++; acc.wen += kd; }
-				else { acc.sheep++; acc.sen += kd; }
-			}
-		}
-		if (o > w.cap) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
-		if (live) {
-			if (CPT == 8) {
-				uint4 q;
-				memcpy(&q, gr, 16);
-				*reinterpret_cast<uint4 *>(gp) = q;
-			} else if (CPT == 4) {
-				uint2 q;
-				memcpy(&q, gr, 8);
-				*reinterpret_cast<uint2 *>(gp) = q;
+				act_cell(p, e, LV, LP, LD, run, lc0 + q, t, gq);
 			} else {
-#pragma unroll
-				for (int q = 0; q < CPT; q += 8) {
-					uint4 v;
-					memcpy(&v, gr + q, 16);
-					*reinterpret_cast<uint4 *>(gp + q) = v;
+				for (uint32_t j = p; j < e; j++) {
+					LV[j] &= TYPE_BIT;
+					LD[j] = 0;
 				}
 			}
 		}
-		__syncthreads();
+		if (real) {
+			acc.galive += gq == 0;
+			acc.gen += gq;
+		}
+		gr[q] = (uint16_t) gq;
+		p = e;
 	}
-	if (cur_run >= 0)
-		flush_stats(acc, &w.ring[(size_t) row * w.nruns_cap + cur_run]);
+	if (live) store_grass<CPT>(gp, gr);
+	/* Survivors + newborns of this thread, in list order. */
+	uint32_t cnt = 0;
+	for (uint32_t j = pbeg; j < pend; j++)
+		cnt += ((LV[j] & ENERGY_MASK) != 0) + (LD[j] != 0);
+	uint32_t total;
+	const uint32_t excl = block_excl_scan(cnt, &total);
+	if (tid < 32) {
+		uint32_t base = warp_lookback(w.lb_act, tile, total, epoch, &w.ctr->err);
+		if (tid == 0) {
+			s_base = base;
+			if (tile == w.n_tiles - 1) w.ctr->n_agents = min(base + total, w.cap);
+		}
+	}
+	__syncthreads();
+	uint32_t o = s_base + excl;
+	for (uint32_t j = pbeg; j < pend; j++) {
+		const uint32_t v = LV[j], k = LK[j], kd = LD[j];
+		const uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
+		if (en) {
+			if (o < w.cap) {
+				w.kA[o] = k;
+				w.vA[o] = v;
+			}
+			o++;
+			if (tb) { acc.wolves++; acc.wen += en; }
+			else { acc.sheep++; acc.sen += en; }
+		}
+		if (kd) {
+			if (o < w.cap) {
+				w.kA[o] = k;
+				w.vA[o] = tb | kd;
+			}
+			o++;
+			if (tb) { acc.wolves++; acc.wen += kd; }
+			else { acc.sheep++; acc.sen += kd; }
+		}
+	}
+	if (o > w.cap) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
+	block_stats(acc, s_part);
+	if (tid < 6) w.part[(size_t) tile * 8 + tid] = s_part[tid];
+}
 
-	/* The last CTA to finish advances the iteration and resets the
-	 * per-launch counters and accumulators for the next iteration. */
+/* Sum the per-tile partial stats per run into the stats ring row of this
+ * iteration; the last CTA advances the iteration and resets the per-launch
+ * counters and accumulators for the next one. */
+__global__ void __launch_bounds__(256) k_finish(WorldDev w)
+{
+	__shared__ uint32_t s_last;
+	__shared__ uint64_t s_part[6];
+	const uint32_t g = w.ctr->giter + 1;
+	const uint32_t row = g % w.ring_rows;
+	const uint32_t per = (w.n_tiles + gridDim.x - 1) / gridDim.x;
+	const uint32_t t0 = blockIdx.x * per;
+	const uint32_t t1 = min(t0 + per, w.n_tiles);
+	const uint32_t r0 = t0 < t1 ? w.tile_run[t0] : 0;
+	bool same = true;
+	for (uint32_t tl = t0 + threadIdx.x; tl < t1; tl += blockDim.x)
+		same &= w.tile_run[tl] == r0;
+	same = __syncthreads_and(same);
+	if (t0 < t1) {
+		if (same) {
+			/* one run: block reduction, one atomic per field */
+			uint64_t v[6] = {0, 0, 0, 0, 0, 0};
+			for (uint32_t tl = t0 + threadIdx.x; tl < t1; tl += blockDim.x) {
+#pragma unroll
+				for (int f = 0; f < 6; f++) v[f] += w.part[(size_t) tl * 8 + f];
+			}
+			StatAcc a;
+			a.sheep = (uint32_t) v[0]; a.wolves = (uint32_t) v[1];
+			a.galive = (uint32_t) v[2]; a.sen = v[3]; a.wen = v[4]; a.gen = v[5];
+			block_stats(a, s_part);
+			if (threadIdx.x < 6)
+				stats_atomic_add(&w.ring[(size_t) row * w.nruns_cap + r0],
+					threadIdx.x, s_part[threadIdx.x]);
+		} else {
+			for (uint32_t tl = t0 + threadIdx.x; tl < t1; tl += blockDim.x) {
+				PPStatistics *dst = &w.ring[(size_t) row * w.nruns_cap + w.tile_run[tl]];
+				for (int f = 0; f < 6; f++)
+					stats_atomic_add(dst, f, w.part[(size_t) tl * 8 + f]);
+			}
+		}
+	}
 	__threadfence();
 	__syncthreads();
-	if (tid == 0) {
+	if (threadIdx.x == 0) {
 		s_last = 0;
-		uint32_t done = atomicAdd(&w.ctr->act_done, 1u);
+		uint32_t done = atomicAdd(&w.ctr->finish_done, 1u);
 		if (done == gridDim.x - 1) {
 			__threadfence();
 			s_last = 1;
 			w.ctr->giter = g;
 			w.ctr->seq = w.ctr->seq + 1;
 			w.ctr->act_ticket = 0;
-			w.ctr->act_done = 0;
+			w.ctr->finish_done = 0;
 			for (int q = 0; q < 8; q++) w.ctr->sort_ticket[q] = 0;
 		}
 	}
 	__syncthreads();
 	if (s_last) {
-		for (uint32_t q = tid; q < 8 * 256; q += ACT_THREADS) w.hist[q] = 0;
+		for (uint32_t q = threadIdx.x; q < 8 * 256; q += blockDim.x) w.hist[q] = 0;
 		const uint32_t nrow = (g + 1) % w.ring_rows;
 		uint32_t *rowp = reinterpret_cast<uint32_t *>(
 			&w.ring[(size_t) nrow * w.nruns_cap]);
 		const uint32_t words = w.nruns_cap * (sizeof(PPStatistics) / 4);
-		for (uint32_t q = tid; q < words; q += ACT_THREADS) rowp[q] = 0;
+		for (uint32_t q = threadIdx.x; q < words; q += blockDim.x) rowp[q] = 0;
+	}
+}
+
+/* After a standalone sort on the world's counters (initial agents, an
+ * admitted run): new look-back epochs, fresh sort tickets and histograms. */
+__global__ void k_after_sort(WorldCounters *ctr, uint32_t *hist)
+{
+	for (uint32_t q = threadIdx.x; q < 8 * 256; q += blockDim.x) hist[q] = 0;
+	if (threadIdx.x == 0) {
+		ctr->seq = ctr->seq + 1;
+		for (int q = 0; q < 8; q++) ctr->sort_ticket[q] = 0;
 	}
 }
 
@@ -478,7 +607,7 @@ __global__ void k_init_grass(WorldDev w, RunDev run)
 		lc += gridDim.x * blockDim.x) {
 		uint16_t v = 0;
 		if (lc < run.ncells) {
-			u4 r = rng(run.seed_lo, run.seed_hi, lc, 0, STREAM_INIT_CELL);
+			u4 r = rng(run.seed_lo, run.seed_hi, lc, 0, STREAM_INIT_CELL, 0);
 			uint32_t alive = draw(r.x, 2);
 			v = alive ? 0 : (uint16_t) (1 + draw(r.y, run.restart));
 		}
@@ -486,19 +615,20 @@ __global__ void k_init_grass(WorldDev w, RunDev run)
 	}
 }
 
-__global__ void k_init_agents(WorldDev w, RunDev run, uint32_t base,
-	uint32_t n_sheep, uint32_t n_wolves)
+/* Initial agents of a run, in creation order, into k/v[base ..). */
+__global__ void k_init_agents(RunDev run, uint32_t *k, uint32_t *v,
+	uint32_t base, uint32_t n_sheep, uint32_t n_wolves)
 {
 	const uint32_t n = n_sheep + n_wolves;
 	for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < n;
 		a += gridDim.x * blockDim.x) {
-		u4 r = rng(run.seed_lo, run.seed_hi, a, 0, STREAM_INIT_AGENT);
+		u4 r = rng(run.seed_lo, run.seed_hi, a, 0, STREAM_INIT_AGENT, 0);
 		uint32_t x = draw(r.x, run.gx), y = draw(r.y, run.gy);
 		bool wolf = a >= n_sheep;
 		uint32_t gain = wolf ? run.wolves_gain : run.sheep_gain;
 		uint32_t e = 1 + draw(r.z, 2 * gain);
-		w.kA[base + a] = run.cbase + y * run.gx + x;
-		w.vA[base + a] = (wolf ? TYPE_BIT : 0u) | e;
+		k[base + a] = run.cbase + y * run.gx + x;
+		v[base + a] = (wolf ? TYPE_BIT : 0u) | e;
 	}
 }
 
@@ -506,6 +636,7 @@ __global__ void k_init_agents(WorldDev w, RunDev run, uint32_t base,
 __global__ void __launch_bounds__(ACT_THREADS) k_stats_run(WorldDev w,
 	RunDev run, uint32_t base, uint32_t n, PPStatistics *dst)
 {
+	__shared__ uint64_t s_part[6];
 	StatAcc acc;
 	acc.zero();
 	const uint32_t stride = gridDim.x * blockDim.x;
@@ -520,7 +651,8 @@ __global__ void __launch_bounds__(ACT_THREADS) k_stats_run(WorldDev w,
 		acc.galive += gq == 0;
 		acc.gen += gq;
 	}
-	flush_stats(acc, dst);
+	block_stats(acc, s_part);
+	if (threadIdx.x < 6) stats_atomic_add(dst, threadIdx.x, s_part[threadIdx.x]);
 }
 
 __global__ void k_philox_fill(uint32_t c0, uint32_t c1, uint32_t c2,
@@ -540,8 +672,9 @@ __global__ void k_philox_fill(uint32_t c0, uint32_t c1, uint32_t c2,
 cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
 	cudaStream_t s, const cudaEvent_t *marks)
 {
-	/* marks (optional, passes + 4 events): before the move, after the
-	 * move, after each radix pass, after the offsets, after the act. */
+	/* marks (optional, passes + 5 events): before the move, after the
+	 * move, after each radix pass, after the offsets, after the act, after
+	 * the finish. */
 	if (marks) cudaEventRecord(marks[0], s);
 	size_t hist_smem = (size_t) (w.passes << w.digit_bits) * sizeof(uint32_t);
 	k_move<<<lc.move_blocks, 256, hist_smem, s>>>(w);
@@ -562,11 +695,14 @@ cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
 	if (marks) cudaEventRecord(marks[2 + w.passes], s);
 	size_t act_smem = (size_t) w.act_cap * 4 * sizeof(uint32_t);
 	switch (lc.cpt) {
-	case 4: k_act<4><<<lc.act_blocks, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
-	case 16: k_act<16><<<lc.act_blocks, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
-	default: k_act<8><<<lc.act_blocks, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
+	case 4: k_act<4><<<w.n_tiles, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
+	case 16: k_act<16><<<w.n_tiles, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
+	case 32: k_act<32><<<w.n_tiles, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
+	default: k_act<8><<<w.n_tiles, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
 	}
 	if (marks) cudaEventRecord(marks[3 + w.passes], s);
+	k_finish<<<lc.finish_blocks, 256, 0, s>>>(w);
+	if (marks) cudaEventRecord(marks[4 + w.passes], s);
 	return cudaGetLastError();
 }
 
@@ -577,29 +713,48 @@ cudaError_t set_act_smem_limits(size_t bytes)
 	if (e != cudaSuccess) return e;
 	e = cudaFuncSetAttribute(k_act<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
 	if (e != cudaSuccess) return e;
-	return cudaFuncSetAttribute(k_act<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+	e = cudaFuncSetAttribute(k_act<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+	if (e != cudaSuccess) return e;
+	return cudaFuncSetAttribute(k_act<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
 }
 
-cudaError_t enqueue_init_run(const WorldDev &w, const LaunchCfg &lc,
-	const RunDev &run, uint32_t r, uint32_t base, uint32_t init_sheep,
-	uint32_t init_wolves, uint32_t row, cudaStream_t s)
+cudaError_t enqueue_init_grass(const WorldDev &w, const RunDev &run,
+	cudaStream_t s)
 {
-	(void) lc;
 	uint32_t span = run.n_tiles << w.log_tile;
 	uint32_t gb = (span + 255) / 256;
 	if (gb > 4096) gb = 4096;
+	if (gb == 0) gb = 1;
 	k_init_grass<<<gb, 256, 0, s>>>(w, run);
+	return cudaGetLastError();
+}
+
+cudaError_t enqueue_init_agents(const RunDev &run, uint32_t *k, uint32_t *v,
+	uint32_t base, uint32_t init_sheep, uint32_t init_wolves, cudaStream_t s)
+{
 	uint32_t n = init_sheep + init_wolves;
-	if (n) {
-		uint32_t ab = (n + 255) / 256;
-		if (ab > 4096) ab = 4096;
-		k_init_agents<<<ab, 256, 0, s>>>(w, run, base, init_sheep, init_wolves);
-	}
+	if (!n) return cudaSuccess;
+	uint32_t ab = (n + 255) / 256;
+	if (ab > 4096) ab = 4096;
+	k_init_agents<<<ab, 256, 0, s>>>(run, k, v, base, init_sheep, init_wolves);
+	return cudaGetLastError();
+}
+
+cudaError_t enqueue_stats_run(const WorldDev &w, const RunDev &run,
+	uint32_t r, uint32_t base, uint32_t n, uint32_t row, cudaStream_t s)
+{
 	uint32_t sb = (max(n, run.ncells) + ACT_THREADS - 1) / ACT_THREADS;
 	if (sb > 1024) sb = 1024;
 	if (sb == 0) sb = 1;
 	k_stats_run<<<sb, ACT_THREADS, 0, s>>>(w, run, base, n,
 		&w.ring[(size_t) row * w.nruns_cap + r]);
+	return cudaGetLastError();
+}
+
+cudaError_t enqueue_after_sort(WorldCounters *ctr, uint32_t *hist,
+	cudaStream_t s)
+{
+	k_after_sort<<<1, 256, 0, s>>>(ctr, hist);
 	return cudaGetLastError();
 }
 
@@ -634,10 +789,6 @@ cudaError_t launch_philox_fill(uint32_t c0, uint32_t c1, uint32_t c2,
 	return cudaGetLastError();
 }
 
-} /* namespace pp */
-
-namespace pp {
-
 int occupancy_act(int cpt, size_t smem)
 {
 	int n = 0;
@@ -645,6 +796,7 @@ int occupancy_act(int cpt, size_t smem)
 	switch (cpt) {
 	case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_act<4>, ACT_THREADS, smem); break;
 	case 16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_act<16>, ACT_THREADS, smem); break;
+	case 32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_act<32>, ACT_THREADS, smem); break;
 	default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_act<8>, ACT_THREADS, smem); break;
 	}
 	if (e != cudaSuccess) { cudaGetLastError(); return 1; }

@@ -10,8 +10,8 @@
 namespace pp {
 
 /* Everything one world iteration touches. Arrays A, B, C are agent
- * key/value arrays of `cap` slots: A = pre-move (canonical order), the
- * move writes B, the radix passes ping-pong B <-> C, the act reads the
+ * key/value arrays of `cap` slots: A = pre-move (cell-sorted cell lists),
+ * the move writes B, the radix passes ping-pong B <-> C, the act reads the
  * sorted array and writes A. */
 struct WorldDev {
 	uint16_t *grass;          /* n_tiles << log_tile cells                 */
@@ -19,13 +19,13 @@ struct WorldDev {
 	uint32_t *tile_off;       /* n_tiles + 1                               */
 	uint16_t *tile_run;       /* n_tiles                                   */
 	RunDev *runs;             /* nruns_cap                                 */
-	uint32_t *run_base;       /* agent base of each run in A               */
 	uint64_t *lb_sort;        /* sort look-back words [max sort tiles][radix] */
 	uint64_t *lb_act;         /* act look-back words [n_tiles]             */
 	WorldCounters *ctr;
 	uint32_t *hist;           /* [8][256] digit counts of the moved keys   */
 	PPStatistics *ring;       /* [ring_rows][nruns_cap]                    */
 	uint32_t *scratch_prio, *scratch_kid; /* [cap], act fallback           */
+	uint64_t *part;           /* [n_tiles][8] per-tile partial stats       */
 	uint32_t cap, n_tiles, log_tile, nruns_cap, ring_rows;
 	uint32_t key_bits, digit_bits, passes;
 	uint32_t act_cap;         /* agents per tile held in shared memory     */
@@ -34,8 +34,8 @@ struct WorldDev {
 
 struct LaunchCfg {
 	int sms;
-	int move_blocks, sort_blocks, act_blocks, offs_blocks;
-	int cpt;                  /* cells per act thread (4, 8 or 16)          */
+	int move_blocks, sort_blocks, offs_blocks, finish_blocks;
+	int cpt;                  /* cells per act thread (4, 8, 16 or 32)      */
 };
 
 /* Sort tile geometry. */
@@ -44,16 +44,24 @@ constexpr int SORT_IPT = 16;
 constexpr int SORT_TILE = SORT_THREADS * SORT_IPT;
 constexpr int ACT_THREADS = 256;
 
-/* One iteration: move, radix passes, tile offsets, act. Returns a CUDA
- * error code (cudaSuccess = 0). */
+/* One iteration: move, radix passes, tile offsets, act, finish. Returns a
+ * CUDA error code (cudaSuccess = 0). */
 cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
 	cudaStream_t s, const cudaEvent_t *marks = nullptr);
 
-/* Initialise run r: grass of its tiles, its initial agents at A[base..),
- * and accumulate its initial stats into ring row `row`. */
-cudaError_t enqueue_init_run(const WorldDev &w, const LaunchCfg &lc,
-	const RunDev &run, uint32_t r, uint32_t base, uint32_t init_sheep,
-	uint32_t init_wolves, uint32_t row, cudaStream_t s);
+/* Initialisation of a run: grass of its tiles; its initial agents in
+ * creation order into k/v[base ..) (sorted by cell afterwards); the stats
+ * of its agents A[base, base + n) and cells into ring row `row`. */
+cudaError_t enqueue_init_grass(const WorldDev &w, const RunDev &run,
+	cudaStream_t s);
+cudaError_t enqueue_init_agents(const RunDev &run, uint32_t *k, uint32_t *v,
+	uint32_t base, uint32_t init_sheep, uint32_t init_wolves, cudaStream_t s);
+cudaError_t enqueue_stats_run(const WorldDev &w, const RunDev &run,
+	uint32_t r, uint32_t base, uint32_t n, uint32_t row, cudaStream_t s);
+/* After a standalone sort that used the world's counters: new look-back
+ * epochs, fresh tickets, zero histograms. */
+cudaError_t enqueue_after_sort(WorldCounters *ctr, uint32_t *hist,
+	cudaStream_t s);
 
 /* Standalone kernels for kernel-level checks. */
 cudaError_t launch_move_only(const uint32_t *kin, const uint32_t *vin,

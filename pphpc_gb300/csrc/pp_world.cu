@@ -48,7 +48,7 @@ void choose_geometry(uint32_t total_cells, uint32_t cap, WorldConfig &cfg)
 		/* Dense worlds (many agents per cell) take smaller tiles so a
 		 * tile's agents fit in shared memory. */
 		double dens = total_cells ? (double) cap / total_cells : 1.0;
-		cfg.tile_cells = dens > 1.0 ? 1024 : 2048;
+		cfg.tile_cells = dens > 1.0 ? 1024 : 4096;
 	}
 	(void) cap;
 }
@@ -127,7 +127,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	choose_geometry((uint32_t) std::min<uint64_t>(total_cells, 0xffffffffu),
 		cfg.cap, cfg);
 	uint32_t T = cfg.tile_cells;
-	if (T != 1024 && T != 2048 && T != 4096) return PP_INVALID_ARGS;
+	if (T != 1024 && T != 2048 && T != 4096 && T != 8192) return PP_INVALID_ARGS;
 	uint32_t log_tile = 0;
 	while ((1u << log_tile) < T) log_tile++;
 
@@ -188,7 +188,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	PP_AL(w_.tile_off, ((size_t) tiles + 1) * 4);
 	PP_AL(w_.tile_run, (size_t) tiles * 2);
 	PP_AL(w_.runs, (size_t) nruns_cap * sizeof(RunDev));
-	PP_AL(w_.run_base, (size_t) nruns_cap * 4);
+	PP_AL(w_.part, (size_t) tiles * 8 * sizeof(uint64_t));
 	size_t sort_tiles = ceil_div(cap, SORT_TILE) + 1;
 	PP_AL(w_.lb_sort, sort_tiles * 256 * sizeof(uint64_t));
 	PP_AL(w_.lb_act, (size_t) tiles * sizeof(uint64_t));
@@ -200,7 +200,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	PP_CK(cudaMemsetAsync(w_.lb_act, 0, (size_t) tiles * sizeof(uint64_t), s_));
 	PP_CK(cudaMemsetAsync(w_.hist, 0, 8 * 256 * 4, s_));
 	PP_CK(cudaMemsetAsync(w_.ring, 0, (size_t) w_.ring_rows * nruns_cap * sizeof(PPStatistics), s_));
-	PP_CK(cudaMemsetAsync(w_.run_base, 0, (size_t) nruns_cap * 4, s_));
+	PP_CK(cudaMemsetAsync(w_.part, 0, (size_t) tiles * 8 * sizeof(uint64_t), s_));
 
 	/* Run table and tile map. */
 	runs_h_.assign(nruns_cap, RunDev{});
@@ -217,29 +217,39 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	if (cfg.extra_tiles) free_tiles_.push_back({used_tiles_, cfg.extra_tiles});
 	PP_CK(cudaMemcpyAsync(w_.runs, runs_h_.data(), nruns_cap * sizeof(RunDev), cudaMemcpyHostToDevice, s_));
 	PP_CK(cudaMemcpyAsync(w_.tile_run, tile_run_h_.data(), tiles * 2, cudaMemcpyHostToDevice, s_));
-	PP_CK(cudaMemcpyAsync(w_.run_base, base_h.data(), nruns_cap * 4, cudaMemcpyHostToDevice, s_));
 	WorldCounters c{};
-	c.n_agents = base;
 	PP_CK(cudaMemcpyAsync(w_.ctr, &c, sizeof(c), cudaMemcpyHostToDevice, s_));
-	h2d_ += nruns_cap * sizeof(RunDev) + tiles * 2 + nruns_cap * 4 + sizeof(c);
+	h2d_ += nruns_cap * sizeof(RunDev) + tiles * 2 + sizeof(c);
 
 	/* Launch geometry. */
 	lc_.sms = sms;
 	lc_.cpt = (int) (T / ACT_THREADS);
 	size_t act_smem = (size_t) act_cap * 16;
 	PP_CK(set_act_smem_limits(act_smem));
-	int occ_act = occupancy_act(lc_.cpt, act_smem);
 	int occ_sort = occupancy_sort((int) d);
-	if (occ_act < 1) occ_act = 1;
 	if (occ_sort < 1) occ_sort = 1;
-	lc_.act_blocks = (int) std::min<uint64_t>(tiles, (uint64_t) sms * occ_act);
 	lc_.sort_blocks = sms * occ_sort;
 	lc_.move_blocks = sms * 8;
 	lc_.offs_blocks = sms * 8;
+	lc_.finish_blocks = (int) std::min<uint64_t>(tiles, (uint64_t) sms * 2);
 
+	/* Initial state: grass, then every run's agents in creation order into
+	 * B at the run's base, sorted by cell into A (runs occupy increasing
+	 * cell ranges, so each run's agents stay at its base), stats row 0. */
 	for (size_t r = 0; r < runs.size(); r++) {
-		rc = cuda_status(enqueue_init_run(w_, lc_, runs_h_[r], (uint32_t) r,
-			base_h[r], runs[r].p.init_sheep, runs[r].p.init_wolves, 0, s_));
+		rc = cuda_status(enqueue_init_grass(w_, runs_h_[r], s_));
+		if (rc) return rc;
+		rc = cuda_status(enqueue_init_agents(runs_h_[r], w_.kB, w_.vB, base_h[r],
+			runs[r].p.init_sheep, runs[r].p.init_wolves, s_));
+		if (rc) return rc;
+	}
+	rc = sort_into(base, w_.kA, w_.vA);
+	if (rc) return rc;
+	PP_CK(cudaMemcpyAsync(&w_.ctr->n_agents, &base, 4, cudaMemcpyHostToDevice, s_));
+	h2d_ += 4;
+	for (size_t r = 0; r < runs.size(); r++) {
+		rc = cuda_status(enqueue_stats_run(w_, runs_h_[r], (uint32_t) r, base_h[r],
+			runs[r].p.init_sheep + runs[r].p.init_wolves, 0, s_));
 		if (rc) return rc;
 	}
 	giter_ = 0;
@@ -249,6 +259,30 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 		rc = build_graph();
 		if (rc) return rc;
 	}
+	return PP_SUCCESS;
+}
+
+int World::sort_into(uint32_t n, uint32_t *dst_k, uint32_t *dst_v)
+{
+	/* Stable radix sort of B[0, n) by cell on the world's counters, then a
+	 * copy to dst; leaves fresh epochs, tickets and histograms. */
+	PP_CK(cudaMemcpyAsync(&w_.ctr->aux_n, &n, 4, cudaMemcpyHostToDevice, s_));
+	h2d_ += 4;
+	if (n) {
+		PP_CK(launch_radix_hist(w_.kB, &w_.ctr->aux_n, w_.hist, w_.digit_bits,
+			w_.passes, lc_.move_blocks, s_));
+		uint32_t *ki = w_.kB, *vi = w_.vB, *ko = w_.kC, *vo = w_.vC;
+		for (uint32_t p = 0; p < w_.passes; p++) {
+			PP_CK(launch_radix_pass(ki, vi, ko, vo, w_.hist + p * 256, w_.lb_sort,
+				w_.ctr, &w_.ctr->aux_n, p, p * w_.digit_bits, w_.digit_bits,
+				lc_.sort_blocks, s_));
+			std::swap(ki, ko);
+			std::swap(vi, vo);
+		}
+		PP_CK(cudaMemcpyAsync(dst_k, ki, (size_t) n * 4, cudaMemcpyDeviceToDevice, s_));
+		PP_CK(cudaMemcpyAsync(dst_v, vi, (size_t) n * 4, cudaMemcpyDeviceToDevice, s_));
+	}
+	PP_CK(enqueue_after_sort(w_.ctr, w_.hist, s_));
 	return PP_SUCCESS;
 }
 
@@ -356,10 +390,10 @@ int World::profile(uint32_t n, pp_kernel_prof *prof, double *agent_steps)
 {
 	PP_CK(cudaSetDevice(device_));
 	const uint32_t P = w_.passes;
-	std::vector<cudaEvent_t> ev(P + 4);
+	std::vector<cudaEvent_t> ev(P + 5);
 	for (auto &e : ev) PP_CK(cudaEventCreate(&e));
-	static const char *names[4] = {"move", "radix_pass", "offsets", "act"};
-	for (int k = 0; k < 4; k++) {
+	static const char *names[5] = {"move", "radix_pass", "offsets", "act", "finish"};
+	for (int k = 0; k < 5; k++) {
 		memset(&prof[k], 0, sizeof(prof[k]));
 		snprintf(prof[k].name, sizeof(prof[k].name), "%s", names[k]);
 	}
@@ -393,6 +427,9 @@ int World::profile(uint32_t n, pp_kernel_prof *prof, double *agent_steps)
 		PP_CK(cudaEventElapsedTime(&ms, ev[2 + P], ev[3 + P]));
 		prof[3].launches++; prof[3].total_ms += ms;
 		prof[3].bytes += 4.0 * live_cells + 8.0 * n_live + 8.0 * n_after;
+		PP_CK(cudaEventElapsedTime(&ms, ev[3 + P], ev[4 + P]));
+		prof[4].launches++; prof[4].total_ms += ms;
+		prof[4].bytes += 48.0 * w_.n_tiles;
 		steps += n_before;
 	}
 	for (auto &e : ev) cudaEventDestroy(e);
@@ -443,15 +480,22 @@ int World::admit(const RunSpec &spec, uint32_t *slot_out)
 	for (uint32_t t = 0; t < need; t++) tile_run_h_[first + t] = (uint16_t) slot;
 	PP_CK(cudaMemcpyAsync(&w_.runs[slot], &run, sizeof(RunDev), cudaMemcpyHostToDevice, s_));
 	PP_CK(cudaMemcpyAsync(&w_.tile_run[first], &tile_run_h_[first], need * 2, cudaMemcpyHostToDevice, s_));
-	PP_CK(cudaMemcpyAsync(&w_.run_base[slot], &n, 4, cudaMemcpyHostToDevice, s_));
 	uint32_t row = giter_ % w_.ring_rows;
 	PP_CK(cudaMemsetAsync(&w_.ring[(size_t) row * w_.nruns_cap + slot], 0, sizeof(PPStatistics), s_));
-	int rc = cuda_status(enqueue_init_run(w_, lc_, run, slot, n,
-		spec.p.init_sheep, spec.p.init_wolves, row, s_));
+	/* Grass of its tiles; its agents sorted by cell and appended to A. The
+	 * other runs' agents stay in place: draws never depend on positions. */
+	int rc = cuda_status(enqueue_init_grass(w_, run, s_));
+	if (rc) return rc;
+	rc = cuda_status(enqueue_init_agents(run, w_.kB, w_.vB, 0,
+		spec.p.init_sheep, spec.p.init_wolves, s_));
+	if (rc) return rc;
+	rc = sort_into(n0, w_.kA + n, w_.vA + n);
+	if (rc) return rc;
+	rc = cuda_status(enqueue_stats_run(w_, run, slot, n, n0, row, s_));
 	if (rc) return rc;
 	uint32_t nn = n + n0;
 	PP_CK(cudaMemcpyAsync(&w_.ctr->n_agents, &nn, 4, cudaMemcpyHostToDevice, s_));
-	h2d_ += sizeof(RunDev) + need * 2 + 4 + 4;
+	h2d_ += sizeof(RunDev) + need * 2 + 4;
 	d2h_ += 4;
 	*slot_out = slot;
 	return PP_SUCCESS;
@@ -651,7 +695,7 @@ extern "C" int pp_sim_get_state(pp_sim *sim, uint32_t *cell, uint32_t *en,
 extern "C" int pp_sim_profile(pp_sim *sim, uint32_t n_iters,
 	pp_kernel_prof *prof, uint32_t n_prof, double *agent_steps)
 {
-	if (!sim || !prof || n_prof < 4) return PP_INVALID_ARGS;
+	if (!sim || !prof || n_prof < 5) return PP_INVALID_ARGS;
 	if (n_iters >= sim->world.ring_rows()) return PP_INVALID_ARGS;
 	return sim->world.profile(n_iters, prof, agent_steps);
 }

@@ -71,12 +71,13 @@ public:
 		uint32_t *n_out, uint16_t *grass, uint32_t r);
 
 	/* Run n iterations without graphs, timing every kernel with CUDA
-	 * events on the world's stream; accumulates into prof[0..3] (move,
-	 * radix pass, offsets, act) with algorithmic bytes. */
+	 * events on the world's stream; fills prof[0..4] (move, radix pass,
+	 * offsets, act, finish) with algorithmic bytes. */
 	int profile(uint32_t n, pp_kernel_prof *prof, double *agent_steps);
 
 private:
 	int alloc(size_t bytes, void **p);
+	int sort_into(uint32_t n, uint32_t *dst_k, uint32_t *dst_v);
 	int build_graph();
 	int init_run_device(uint32_t r, uint32_t base, const RunSpec &spec);
 	void free_all();

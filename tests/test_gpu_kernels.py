@@ -29,7 +29,8 @@ def test_philox_million_counters():
 
 
 def _agents(rng, p, n):
-    cell = rng.integers(0, p.grid_x * p.grid_y, n, dtype=np.uint32)
+    # cell-sorted, as the move's input always is (ranks within cells key the draws)
+    cell = np.sort(rng.integers(0, p.grid_x * p.grid_y, n, dtype=np.uint32))
     e = rng.integers(0, 60, n, dtype=np.uint32)
     t = rng.integers(0, 2, n, dtype=np.uint32) << np.uint32(31)
     return cell, e | t
@@ -44,6 +45,8 @@ def test_move_matches_oracle(gx, gy):
     # put agents on all four borders and corners
     cell[:4] = [0, gx - 1, (gy - 1) * gx, gx * gy - 1]
     en[:4] = 10
+    order = np.argsort(cell, kind="stable")
+    cell, en = cell[order], en[order]
     for it in (1, 2, 4000):
         gc, ge = pp.move(p, 99, it, cell, en)
         oc, oe = orc.move(p, 99, it, cell, en)

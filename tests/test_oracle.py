@@ -132,7 +132,7 @@ def test_act_closed_form_matches_sequential_lists(case):
     pr = {}
     dice = {}
     for s in range(m):
-        w = orc.philox((s, it, 3, 0), (seed, 0))
+        w = orc.philox((7, it, 3, s), (seed, 0))  # cell 7, act stream, rank s
         pr[s] = w[0]
         dice[s] = orc.draw(w[1], 100)
     order = sorted(range(m), key=lambda s: (pr[s], s))
