@@ -130,9 +130,10 @@ struct RunDev {
 	fastdiv gxdiv;
 };
 
-/* Per-world counters in device memory. The act kernel's last CTA advances
- * the iteration and resets the per-launch counters for the next one, so a
- * whole iteration is a fixed launch sequence (capturable as a graph). */
+/* Per-world counters in device memory. The finish kernel's last CTA
+ * advances the iteration and resets the per-launch counters for the next
+ * one, so a whole iteration is a fixed launch sequence (captured as a
+ * graph). */
 struct WorldCounters {
 	uint32_t n_agents;       /* live agents in the pre-move array        */
 	uint32_t giter;          /* world iterations completed               */
@@ -142,7 +143,8 @@ struct WorldCounters {
 	uint32_t finish_done;    /* finish CTAs done                          */
 	uint32_t sort_ticket[8]; /* one per radix pass                        */
 	uint32_t aux_n;          /* element count of a standalone sort        */
-	uint32_t pad[3];
+	uint32_t fin_ticket;     /* finish chunk tickets                      */
+	uint32_t pad[2];
 };
 
 /* ---- memory-ordering helpers ---- */

@@ -1,21 +1,24 @@
 /*
  * pp_kernels.cu -- the per-iteration simulation kernels for sm_103a.
  *
- *   k_move        move_agent (opencl/pp/pp_gpu.cl:744-821) plus the digit
- *                 histograms of every radix pass (replaces the upfront
- *                 histogram pass of the sort).
+ *   k_regions     move_agent (opencl/pp/pp_gpu.cl:744-821): the agents of
+ *                 each tile's region, moved into the dense sort input, plus
+ *                 the digit histograms of every radix pass (replaces the
+ *                 upfront histogram pass of the sort).
  *   k_offsets     find_cell_idx (pp_gpu.cl:834-867): start index of every
  *                 bucket (a tile of cells, or a single cell) in the
  *                 cell-sorted agent array.
  *   k_act         grass (pp_gpu.cl:448-476) + action_agent
  *                 (pp_gpu.cl:883-979), fused per tile of cells: countdown,
  *                 in-cell conflict resolution in priority order, newborn
- *                 slots by a block prefix sum, compaction of survivors and
- *                 newborns with a warp-wide decoupled look-back across
- *                 tiles, and per-tile partial stats.
+ *                 slots by a block prefix sum, survivors and newborns
+ *                 written to the tile's own region (no inter-tile wait),
+ *                 per-tile partial stats.
  *   k_finish      reduce_grass1/2 + reduce_agent1/2 (pp_gpu.cl:485-736):
- *                 the per-tile partial stats summed per run into the stats
- *                 ring; its last CTA advances the iteration.
+ *                 per-tile partial stats summed per run into the stats
+ *                 ring; scan of the region counts into dense bases
+ *                 (decoupled look-back across chunks of tiles); its last
+ *                 CTA advances the iteration.
  *   k_init_*      init_cell / init_agent (pp_gpu.cl:368-439).
  *
  * Draws are keyed by (cell, rank of the agent in its cell's list), never by
@@ -61,77 +64,84 @@ __device__ __forceinline__ bool run_live(const RunDev &run, uint32_t t)
 	return run.active && t >= 1 && t <= run.iters;
 }
 
-/* Rank of each lane's agent in its cell's list, for a warp holding the
- * consecutive, cell-sorted slots base .. base + 31 of `keys` (lanes past
- * n hold invalid slots). Lane 0 counts the run of equal keys before the
- * warp; the rest follows from a ballot of run starts. */
-__device__ __forceinline__ uint32_t warp_cell_rank(const uint32_t *keys,
-	uint32_t i, uint32_t key, bool valid, uint32_t lane)
-{
-	uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
-	bool start = (lane == 0) ? true : (key != prev);
-	uint32_t starts = __ballot_sync(0xffffffffu, start && valid);
-	uint32_t r0 = 0;
-	if (lane == 0 && valid) {
-		uint32_t j = i;
-		while (j > 0 && keys[j - 1] == key) { j--; r0++; }
-	}
-	r0 = __shfl_sync(0xffffffffu, r0, 0);
-	uint32_t upto = starts & (0xffffffffu >> (31 - lane));
-	uint32_t s = 31 - __clz(upto);   /* last run start at or before lane */
-	return s == 0 ? r0 + lane : lane - s;
-}
-
-__global__ void __launch_bounds__(256) k_move(WorldDev w)
+/* One warp per tile region: the tile's agents (cell-sorted lists) from the
+ * region buffer. MOVE: the move of every agent (draw keyed by cell and
+ * rank in the cell's list; ranks from a ballot of list starts with a carry
+ * across 32-agent chunks) into the dense sort input B at the tile's dense
+ * base, plus the digit histograms of every radix pass. !MOVE: a plain copy
+ * into the dense array ko/vo (state read-back). */
+template <bool MOVE>
+__global__ void __launch_bounds__(256) k_regions(WorldDev w, uint32_t *ko,
+	uint32_t *vo)
 {
 	extern __shared__ uint32_t sh_hist[];
 	const uint32_t d = w.digit_bits, P = w.passes, mask = (1u << d) - 1;
-	for (uint32_t q = threadIdx.x; q < (P << d); q += blockDim.x)
-		sh_hist[q] = 0;
-	__syncthreads();
-	const uint32_t n = w.ctr->n_agents;
+	if (MOVE) {
+		for (uint32_t q = threadIdx.x; q < (P << d); q += blockDim.x)
+			sh_hist[q] = 0;
+		__syncthreads();
+	}
 	const uint32_t g = w.ctr->giter + 1;
 	const uint32_t lane = threadIdx.x & 31;
-	const uint32_t stride = gridDim.x * blockDim.x;
-	for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-		const uint32_t i = base + threadIdx.x;
-		const bool valid = i < n;
-		uint32_t key = valid ? w.kA[i] : 0xffffffffu;
-		uint32_t val = valid ? w.vA[i] : 0;
-		uint32_t k = warp_cell_rank(w.kA, i, key, valid, lane);
-		uint32_t nk = 0xffffffffu, nv = 0;
-		if (valid) {
-			uint32_t r = w.tile_run[key >> w.log_tile];
-			const RunDev &run = w.runs[r];
-			uint32_t t = g - run.start_giter;
-			if (run_live(run, t)) {
-				move_one(run, key, val, k, t, w.dead_key, nk, nv);
-			} else {
-				nk = w.dead_key;
-				nv = val & TYPE_BIT;
+	const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+	for (uint32_t tile = gw; tile < w.n_tiles; tile += nw) {
+		const uint32_t cnt = w.rcnt[tile];
+		if (cnt == 0) continue;
+		const uint32_t rs = w.rstart[tile], db = w.dbase[tile];
+		const RunDev &run = w.runs[w.tile_run[tile]];
+		const uint32_t t = g - run.start_giter;
+		const bool live = run_live(run, t);
+		uint32_t carry_key = 0xffffffffu, carry_rank = 0;
+		for (uint32_t j0 = 0; j0 < cnt; j0 += 32) {
+			const uint32_t j = j0 + lane;
+			const bool valid = j < cnt;
+			const uint32_t key = valid ? w.kR[rs + j] : 0xffffffffu;
+			const uint32_t val = valid ? w.vR[rs + j] : 0;
+			uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+			if (lane == 0) prev = carry_key;
+			const uint32_t starts = __ballot_sync(0xffffffffu, valid && key != prev);
+			const uint32_t upto = starts & (0xffffffffu >> (31 - lane));
+			const uint32_t k = upto ? lane - (31 - __clz(upto)) : carry_rank + 1 + lane;
+			const uint32_t last = min(31u, cnt - j0 - 1);
+			carry_key = __shfl_sync(0xffffffffu, key, last);
+			carry_rank = __shfl_sync(0xffffffffu, k, last);
+			if (!MOVE) {
+				if (valid) {
+					ko[db + j] = key;
+					vo[db + j] = val;
+				}
+				continue;
 			}
-			w.kB[i] = nk;
-			w.vB[i] = nv;
-		}
-		/* Digit counts: one atomic per warp when the warp's digits agree
-		 * (the high digits of a nearly cell-sorted array), else one per
-		 * lane. */
-		for (uint32_t p = 0; p < P; p++) {
-			uint32_t dig = (nk >> (p * d)) & mask;
-			uint32_t d0 = __shfl_sync(0xffffffffu, dig, 0);
-			uint32_t vmask = __ballot_sync(0xffffffffu, valid);
-			bool same = __all_sync(0xffffffffu, !valid || dig == d0);
-			if (same) {
-				if (lane == 0 && vmask) atomicAdd(&sh_hist[(p << d) + d0], __popc(vmask));
-			} else if (valid) {
-				atomicAdd(&sh_hist[(p << d) + dig], 1u);
+			uint32_t nk = 0xffffffffu, nv = 0;
+			if (valid) {
+				if (live) move_one(run, key, val, k, t, w.dead_key, nk, nv);
+				else { nk = w.dead_key; nv = val & TYPE_BIT; }
+				w.kB[db + j] = nk;
+				w.vB[db + j] = nv;
+			}
+			/* Digit counts: one atomic per warp when the warp's digits
+			 * agree (the high digits of a nearly cell-sorted array), else
+			 * one per lane. */
+			const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+			for (uint32_t p = 0; p < P; p++) {
+				uint32_t dig = (nk >> (p * d)) & mask;
+				uint32_t d0 = __shfl_sync(0xffffffffu, dig, 0);
+				bool same = __all_sync(0xffffffffu, !valid || dig == d0);
+				if (same) {
+					if (lane == 0) atomicAdd(&sh_hist[(p << d) + d0], __popc(vmask));
+				} else if (valid) {
+					atomicAdd(&sh_hist[(p << d) + dig], 1u);
+				}
 			}
 		}
 	}
-	__syncthreads();
-	for (uint32_t q = threadIdx.x; q < (P << d); q += blockDim.x) {
-		uint32_t c = sh_hist[q];
-		if (c) atomicAdd(&w.hist[(q >> d) * 256 + (q & mask)], c);
+	if (MOVE) {
+		__syncthreads();
+		for (uint32_t q = threadIdx.x; q < (P << d); q += blockDim.x) {
+			uint32_t c = sh_hist[q];
+			if (c) atomicAdd(&w.hist[(q >> d) * 256 + (q & mask)], c);
+		}
 	}
 }
 
@@ -194,7 +204,7 @@ __global__ void k_offsets(const uint32_t *keys, const uint32_t *n_dev,
  * are no more than the sheep before it.
  * On return LV[j] holds type | final energy (energy 0 = eaten) and LD[j]
  * the newborn's energy (0 = none). */
-__device__ __forceinline__ void act_cell(uint32_t p, uint32_t e,
+__device__ __noinline__ void act_cell(uint32_t p, uint32_t e,
 	uint32_t *LV, uint32_t *LP, uint32_t *LD, const RunDev &run,
 	uint32_t lc, uint32_t t, uint32_t &g)
 {
@@ -410,7 +420,7 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	extern __shared__ uint32_t sm[];
 	uint32_t *sk = sm, *sv = sm + w.act_cap, *sp = sv + w.act_cap,
 		*sd = sp + w.act_cap;
-	__shared__ uint32_t s_tile, s_base;
+	__shared__ uint32_t s_tile;
 	__shared__ uint64_t s_part[6];
 	const uint32_t tid = threadIdx.x;
 	if (tid == 0) s_tile = atomicAdd(&w.ctr->act_ticket, 1u);
@@ -418,11 +428,19 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	const uint32_t tile = s_tile;
 	if (tile >= w.n_tiles) return;
 	const uint32_t g = w.ctr->giter + 1;
-	const uint32_t epoch = w.ctr->seq * 8u + 7u;
 	const uint32_t r = w.tile_run[tile];
 	const RunDev run = w.runs[r];
 	const uint32_t t = g - run.start_giter;
 	const bool live = run_live(run, t);
+	if (!live) {
+		/* finished run or free tile space: no agents survive, no stats */
+		if (tid == 0) {
+			w.rstart[tile] = 0;
+			w.rcnt[tile] = 0;
+		}
+		if (tid < 8) w.part[(size_t) tile * 8 + tid] = 0;
+		return;
+	}
 	const uint32_t c0 = tile << w.log_tile;
 	const uint32_t cell0 = tid * CPT;
 	uint16_t gr[CPT];
@@ -448,95 +466,105 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	StatAcc acc;
 	acc.zero();
 	const uint32_t lc0 = c0 - run.cbase + cell0;
-	const uint32_t pbeg = lower_bound_u32(LK, m, c0 + cell0);
-	const uint32_t pend = lower_bound_u32(LK, m, c0 + cell0 + CPT);
-	uint32_t p = pbeg;
+	/* Countdown of this thread's cells into its slice of shared memory
+	 * (cells past the run's grid are padding and stay untouched). */
+	uint16_t *sg = reinterpret_cast<uint16_t *>(sd + w.act_cap) + cell0;
 #pragma unroll
 	for (int q = 0; q < CPT; q++) {
-		const uint32_t cell = c0 + cell0 + q;
-		const bool real = live && (lc0 + q) < run.ncells;
 		uint32_t gq = gr[q];
-		if (real && gq > 0) gq--;
-		uint32_t e = p;
+		if (gq > 0 && (lc0 + q) < run.ncells) gq--;
+		sg[q] = (uint16_t) gq;
+	}
+	const uint32_t pbeg = lower_bound_u32(LK, m, c0 + cell0);
+	const uint32_t pend = lower_bound_u32(LK, m, c0 + cell0 + CPT);
+	/* Actions, occupied cells only. */
+	for (uint32_t p = pbeg; p < pend;) {
+		const uint32_t cell = LK[p];
+		uint32_t e = p + 1;
 		while (e < pend && LK[e] == cell) e++;
-		if (e > p) {
-			if (real) {
-				act_cell(p, e, LV, LP, LD, run, lc0 + q, t, gq);
-			} else {
-				for (uint32_t j = p; j < e; j++) {
-					LV[j] &= TYPE_BIT;
-					LD[j] = 0;
-				}
-			}
-		}
-		if (real) {
+		const uint32_t q = cell - (c0 + cell0);
+		uint32_t gq = sg[q];
+		act_cell(p, e, LV, LP, LD, run, lc0 + q, t, gq);
+		sg[q] = (uint16_t) gq;
+		p = e;
+	}
+#pragma unroll
+	for (int q = 0; q < CPT; q++) {
+		const uint32_t gq = sg[q];
+		if ((lc0 + q) < run.ncells) {
 			acc.galive += gq == 0;
 			acc.gen += gq;
 		}
 		gr[q] = (uint16_t) gq;
-		p = e;
 	}
-	if (live) store_grass<CPT>(gp, gr);
+	store_grass<CPT>(gp, gr);
 	/* Survivors + newborns of this thread, in list order. */
 	uint32_t cnt = 0;
 	for (uint32_t j = pbeg; j < pend; j++)
 		cnt += ((LV[j] & ENERGY_MASK) != 0) + (LD[j] != 0);
+	/* The tile's next lists go to its own region of the region buffer,
+	 * [2 * a0, 2 * a0 + total): at most two outputs per input agent, so
+	 * regions never overlap and no tile waits for another. The dense
+	 * position of each region comes from the scan in k_finish. */
 	uint32_t total;
 	const uint32_t excl = block_excl_scan(cnt, &total);
-	if (tid < 32) {
-		uint32_t base = warp_lookback(w.lb_act, tile, total, epoch, &w.ctr->err);
-		if (tid == 0) {
-			s_base = base;
-			if (tile == w.n_tiles - 1) w.ctr->n_agents = min(base + total, w.cap);
-		}
+	const uint32_t rs = 2 * a0;
+	if (tid == 0) {
+		w.rstart[tile] = rs;
+		w.rcnt[tile] = total;
 	}
-	__syncthreads();
-	uint32_t o = s_base + excl;
+	uint32_t o = rs + excl;
 	for (uint32_t j = pbeg; j < pend; j++) {
 		const uint32_t v = LV[j], k = LK[j], kd = LD[j];
 		const uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
 		if (en) {
-			if (o < w.cap) {
-				w.kA[o] = k;
-				w.vA[o] = v;
-			}
+			w.kR[o] = k;
+			w.vR[o] = v;
 			o++;
 			if (tb) { acc.wolves++; acc.wen += en; }
 			else { acc.sheep++; acc.sen += en; }
 		}
 		if (kd) {
-			if (o < w.cap) {
-				w.kA[o] = k;
-				w.vA[o] = tb | kd;
-			}
+			w.kR[o] = k;
+			w.vR[o] = tb | kd;
 			o++;
 			if (tb) { acc.wolves++; acc.wen += kd; }
 			else { acc.sheep++; acc.sen += kd; }
 		}
 	}
-	if (o > w.cap) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
 	block_stats(acc, s_part);
 	if (tid < 6) w.part[(size_t) tile * 8 + tid] = s_part[tid];
 }
 
-/* Sum the per-tile partial stats per run into the stats ring row of this
- * iteration; the last CTA advances the iteration and resets the per-launch
- * counters and accumulators for the next one. */
+/* Per chunk of tiles (chunks taken by ticket, so a chunk's predecessors are
+ * always running or done):
+ *   FULL: the chunk's per-tile partial stats summed per run into this
+ *         iteration's stats ring row (reduce_grass/agent, pp_gpu.cl:485-736);
+ *   the exclusive scan of the tiles' region counts into their dense bases
+ *   (decoupled look-back across chunks); the total becomes n_agents, and a
+ *   total above the agent pool raises ERRF_OVERFLOW (pp_gpu.c:847-852);
+ *   the last CTA resets the per-launch counters (FULL: advances the
+ *   iteration, clears the histograms and the next stats row). */
+template <bool FULL>
 __global__ void __launch_bounds__(256) k_finish(WorldDev w)
 {
-	__shared__ uint32_t s_last;
+	__shared__ uint32_t s_chunk, s_last, s_base;
 	__shared__ uint64_t s_part[6];
+	if (threadIdx.x == 0) s_chunk = atomicAdd(&w.ctr->fin_ticket, 1u);
+	__syncthreads();
+	const uint32_t chunk = s_chunk;
 	const uint32_t g = w.ctr->giter + 1;
 	const uint32_t row = g % w.ring_rows;
+	const uint32_t epoch = w.ctr->seq * 8u + 7u;
 	const uint32_t per = (w.n_tiles + gridDim.x - 1) / gridDim.x;
-	const uint32_t t0 = blockIdx.x * per;
+	const uint32_t t0 = min(chunk * per, w.n_tiles);
 	const uint32_t t1 = min(t0 + per, w.n_tiles);
-	const uint32_t r0 = t0 < t1 ? w.tile_run[t0] : 0;
-	bool same = true;
-	for (uint32_t tl = t0 + threadIdx.x; tl < t1; tl += blockDim.x)
-		same &= w.tile_run[tl] == r0;
-	same = __syncthreads_and(same);
-	if (t0 < t1) {
+	if (FULL) {
+		const uint32_t r0 = t0 < t1 ? w.tile_run[t0] : 0;
+		bool same = true;
+		for (uint32_t tl = t0 + threadIdx.x; tl < t1; tl += blockDim.x)
+			same &= w.tile_run[tl] == r0;
+		same = __syncthreads_and(same);
 		if (same) {
 			/* one run: block reduction, one atomic per field */
 			uint64_t v[6] = {0, 0, 0, 0, 0, 0};
@@ -548,7 +576,7 @@ __global__ void __launch_bounds__(256) k_finish(WorldDev w)
 			a.sheep = (uint32_t) v[0]; a.wolves = (uint32_t) v[1];
 			a.galive = (uint32_t) v[2]; a.sen = v[3]; a.wen = v[4]; a.gen = v[5];
 			block_stats(a, s_part);
-			if (threadIdx.x < 6)
+			if (threadIdx.x < 6 && t0 < t1)
 				stats_atomic_add(&w.ring[(size_t) row * w.nruns_cap + r0],
 					threadIdx.x, s_part[threadIdx.x]);
 		} else {
@@ -559,6 +587,29 @@ __global__ void __launch_bounds__(256) k_finish(WorldDev w)
 			}
 		}
 	}
+	/* dense bases of the regions */
+	const uint32_t tpt = (per + blockDim.x - 1) / blockDim.x;
+	const uint32_t ta = min(t0 + threadIdx.x * tpt, t1), tb = min(ta + tpt, t1);
+	uint32_t local = 0;
+	for (uint32_t tl = ta; tl < tb; tl++) local += w.rcnt[tl];
+	uint32_t total;
+	const uint32_t excl = block_excl_scan(local, &total);
+	if (threadIdx.x < 32) {
+		uint32_t base = warp_lookback(w.lb_fin, chunk, total, epoch, &w.ctr->err);
+		if (threadIdx.x == 0) s_base = base;
+	}
+	__syncthreads();
+	uint32_t run = s_base + excl;
+	for (uint32_t tl = ta; tl < tb; tl++) {
+		w.dbase[tl] = run;
+		run += w.rcnt[tl];
+	}
+	if (chunk == gridDim.x - 1 && threadIdx.x == 0) {
+		const uint32_t n = s_base + total;
+		w.dbase[w.n_tiles] = n;
+		if (n > w.cap) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
+		w.ctr->n_agents = min(n, w.cap);
+	}
 	__threadfence();
 	__syncthreads();
 	if (threadIdx.x == 0) {
@@ -567,21 +618,37 @@ __global__ void __launch_bounds__(256) k_finish(WorldDev w)
 		if (done == gridDim.x - 1) {
 			__threadfence();
 			s_last = 1;
-			w.ctr->giter = g;
+			if (FULL) {
+				w.ctr->giter = g;
+				w.ctr->act_ticket = 0;
+				for (int q = 0; q < 8; q++) w.ctr->sort_ticket[q] = 0;
+			}
 			w.ctr->seq = w.ctr->seq + 1;
-			w.ctr->act_ticket = 0;
+			w.ctr->fin_ticket = 0;
 			w.ctr->finish_done = 0;
-			for (int q = 0; q < 8; q++) w.ctr->sort_ticket[q] = 0;
 		}
 	}
 	__syncthreads();
-	if (s_last) {
+	if (FULL && s_last) {
 		for (uint32_t q = threadIdx.x; q < 8 * 256; q += blockDim.x) w.hist[q] = 0;
 		const uint32_t nrow = (g + 1) % w.ring_rows;
 		uint32_t *rowp = reinterpret_cast<uint32_t *>(
 			&w.ring[(size_t) nrow * w.nruns_cap]);
 		const uint32_t words = w.nruns_cap * (sizeof(PPStatistics) / 4);
 		for (uint32_t q = threadIdx.x; q < words; q += blockDim.x) rowp[q] = 0;
+	}
+}
+
+/* Regions of tiles [first, first + count) from the tile offsets of a
+ * cell-sorted array placed at `base` of the region buffer. */
+__global__ void k_regions_set(WorldDev w, uint32_t first, uint32_t count,
+	uint32_t base)
+{
+	for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count;
+		q += gridDim.x * blockDim.x) {
+		const uint32_t t = first + q;
+		w.rstart[t] = base + w.tile_off[t];
+		w.rcnt[t] = w.tile_off[t + 1] - w.tile_off[t];
 	}
 }
 
@@ -632,16 +699,16 @@ __global__ void k_init_agents(RunDev run, uint32_t *k, uint32_t *v,
 	}
 }
 
-/* Stats of a run's current state: agents A[base, base + n), its cells. */
+/* Stats of a run's current state: its agents vals[0, n), its cells. */
 __global__ void __launch_bounds__(ACT_THREADS) k_stats_run(WorldDev w,
-	RunDev run, uint32_t base, uint32_t n, PPStatistics *dst)
+	RunDev run, const uint32_t *vals, uint32_t n, PPStatistics *dst)
 {
 	__shared__ uint64_t s_part[6];
 	StatAcc acc;
 	acc.zero();
 	const uint32_t stride = gridDim.x * blockDim.x;
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-		uint32_t v = w.vA[base + i], en = v & ENERGY_MASK;
+		uint32_t v = vals[i], en = v & ENERGY_MASK;
 		if (v & TYPE_BIT) { acc.wolves++; acc.wen += en; }
 		else { acc.sheep++; acc.sen += en; }
 	}
@@ -677,7 +744,7 @@ cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
 	 * the finish. */
 	if (marks) cudaEventRecord(marks[0], s);
 	size_t hist_smem = (size_t) (w.passes << w.digit_bits) * sizeof(uint32_t);
-	k_move<<<lc.move_blocks, 256, hist_smem, s>>>(w);
+	k_regions<true><<<lc.move_blocks, 256, hist_smem, s>>>(w, w.kB, w.vB);
 	if (marks) cudaEventRecord(marks[1], s);
 	uint32_t *ki = w.kB, *vi = w.vB, *ko = w.kC, *vo = w.vC;
 	for (uint32_t p = 0; p < w.passes; p++) {
@@ -693,7 +760,8 @@ cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
 	k_offsets<<<lc.offs_blocks, 256, 0, s>>>(ki, &w.ctr->n_agents,
 		w.log_tile, w.n_tiles, w.tile_off);
 	if (marks) cudaEventRecord(marks[2 + w.passes], s);
-	size_t act_smem = (size_t) w.act_cap * 4 * sizeof(uint32_t);
+	size_t act_smem = (size_t) w.act_cap * 4 * sizeof(uint32_t)
+		+ ((size_t) lc.cpt * ACT_THREADS) * sizeof(uint16_t);
 	switch (lc.cpt) {
 	case 4: k_act<4><<<w.n_tiles, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
 	case 16: k_act<16><<<w.n_tiles, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
@@ -701,7 +769,7 @@ cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
 	default: k_act<8><<<w.n_tiles, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
 	}
 	if (marks) cudaEventRecord(marks[3 + w.passes], s);
-	k_finish<<<lc.finish_blocks, 256, 0, s>>>(w);
+	k_finish<true><<<lc.finish_blocks, 256, 0, s>>>(w);
 	if (marks) cudaEventRecord(marks[4 + w.passes], s);
 	return cudaGetLastError();
 }
@@ -741,13 +809,36 @@ cudaError_t enqueue_init_agents(const RunDev &run, uint32_t *k, uint32_t *v,
 }
 
 cudaError_t enqueue_stats_run(const WorldDev &w, const RunDev &run,
-	uint32_t r, uint32_t base, uint32_t n, uint32_t row, cudaStream_t s)
+	uint32_t r, const uint32_t *vals, uint32_t n, uint32_t row, cudaStream_t s)
 {
 	uint32_t sb = (max(n, run.ncells) + ACT_THREADS - 1) / ACT_THREADS;
 	if (sb > 1024) sb = 1024;
 	if (sb == 0) sb = 1;
-	k_stats_run<<<sb, ACT_THREADS, 0, s>>>(w, run, base, n,
+	k_stats_run<<<sb, ACT_THREADS, 0, s>>>(w, run, vals, n,
 		&w.ring[(size_t) row * w.nruns_cap + r]);
+	return cudaGetLastError();
+}
+
+cudaError_t enqueue_regions_from_sorted(const WorldDev &w, const LaunchCfg &lc,
+	const uint32_t *sorted_keys, uint32_t first, uint32_t count,
+	uint32_t base, cudaStream_t s)
+{
+	/* tile offsets of the sorted agents (count from ctr->aux_n), regions of
+	 * the given tiles, then dense bases of all regions */
+	k_offsets<<<lc.offs_blocks, 256, 0, s>>>(sorted_keys, &w.ctr->aux_n,
+		w.log_tile, w.n_tiles, w.tile_off);
+	uint32_t b = (count + 255) / 256;
+	if (b == 0) b = 1;
+	if (b > 4096) b = 4096;
+	k_regions_set<<<b, 256, 0, s>>>(w, first, count, base);
+	k_finish<false><<<lc.finish_blocks, 256, 0, s>>>(w);
+	return cudaGetLastError();
+}
+
+cudaError_t enqueue_compact(const WorldDev &w, const LaunchCfg &lc,
+	uint32_t *ko, uint32_t *vo, cudaStream_t s)
+{
+	k_regions<false><<<lc.move_blocks, 256, 0, s>>>(w, ko, vo);
 	return cudaGetLastError();
 }
 

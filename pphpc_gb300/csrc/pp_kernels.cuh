@@ -9,18 +9,23 @@
 
 namespace pp {
 
-/* Everything one world iteration touches. Arrays A, B, C are agent
- * key/value arrays of `cap` slots: A = pre-move (cell-sorted cell lists),
- * the move writes B, the radix passes ping-pong B <-> C, the act reads the
- * sorted array and writes A. */
+/* Everything one world iteration touches. The state between iterations is
+ * the region buffer R: tile t's agents (its cells' lists, cell-sorted) at
+ * [rstart[t], rstart[t] + rcnt[t]), with dense base dbase[t]. The move
+ * reads the regions into the dense array B, the radix passes ping-pong
+ * B <-> C, the act reads the sorted array and writes each tile's region
+ * at twice its sorted offset. A (cap slots) is a dense copy for read-back. */
 struct WorldDev {
 	uint16_t *grass;          /* n_tiles << log_tile cells                 */
 	uint32_t *kA, *vA, *kB, *vB, *kC, *vC;
+	uint32_t *kR, *vR;        /* region buffer, 3 * cap slots              */
+	uint32_t *rstart, *rcnt;  /* n_tiles                                   */
+	uint32_t *dbase;          /* n_tiles + 1                               */
 	uint32_t *tile_off;       /* n_tiles + 1                               */
 	uint16_t *tile_run;       /* n_tiles                                   */
 	RunDev *runs;             /* nruns_cap                                 */
 	uint64_t *lb_sort;        /* sort look-back words [max sort tiles][radix] */
-	uint64_t *lb_act;         /* act look-back words [n_tiles]             */
+	uint64_t *lb_fin;         /* finish look-back words [n_tiles + 1]      */
 	WorldCounters *ctr;
 	uint32_t *hist;           /* [8][256] digit counts of the moved keys   */
 	PPStatistics *ring;       /* [ring_rows][nruns_cap]                    */
@@ -57,7 +62,16 @@ cudaError_t enqueue_init_grass(const WorldDev &w, const RunDev &run,
 cudaError_t enqueue_init_agents(const RunDev &run, uint32_t *k, uint32_t *v,
 	uint32_t base, uint32_t init_sheep, uint32_t init_wolves, cudaStream_t s);
 cudaError_t enqueue_stats_run(const WorldDev &w, const RunDev &run,
-	uint32_t r, uint32_t base, uint32_t n, uint32_t row, cudaStream_t s);
+	uint32_t r, const uint32_t *vals, uint32_t n, uint32_t row, cudaStream_t s);
+/* Regions of tiles [first, first + count) for a cell-sorted array of
+ * ctr->aux_n agents at region-buffer offset `base`, then the dense bases
+ * of all regions. */
+cudaError_t enqueue_regions_from_sorted(const WorldDev &w, const LaunchCfg &lc,
+	const uint32_t *sorted_keys, uint32_t first, uint32_t count,
+	uint32_t base, cudaStream_t s);
+/* Dense copy of all regions into ko/vo (dbase order). */
+cudaError_t enqueue_compact(const WorldDev &w, const LaunchCfg &lc,
+	uint32_t *ko, uint32_t *vo, cudaStream_t s);
 /* After a standalone sort that used the world's counters: new look-back
  * epochs, fresh tickets, zero histograms. */
 cudaError_t enqueue_after_sort(WorldCounters *ctr, uint32_t *hist,

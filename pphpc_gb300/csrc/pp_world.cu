@@ -184,20 +184,26 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	PP_AL(w_.kA, cap * 4); PP_AL(w_.vA, cap * 4);
 	PP_AL(w_.kB, cap * 4); PP_AL(w_.vB, cap * 4);
 	PP_AL(w_.kC, cap * 4); PP_AL(w_.vC, cap * 4);
+	PP_AL(w_.kR, 3 * cap * 4); PP_AL(w_.vR, 3 * cap * 4);
 	PP_AL(w_.scratch_prio, cap * 4); PP_AL(w_.scratch_kid, cap * 4);
+	PP_AL(w_.rstart, (size_t) tiles * 4);
+	PP_AL(w_.rcnt, (size_t) tiles * 4);
+	PP_AL(w_.dbase, ((size_t) tiles + 1) * 4);
 	PP_AL(w_.tile_off, ((size_t) tiles + 1) * 4);
 	PP_AL(w_.tile_run, (size_t) tiles * 2);
 	PP_AL(w_.runs, (size_t) nruns_cap * sizeof(RunDev));
 	PP_AL(w_.part, (size_t) tiles * 8 * sizeof(uint64_t));
 	size_t sort_tiles = ceil_div(cap, SORT_TILE) + 1;
 	PP_AL(w_.lb_sort, sort_tiles * 256 * sizeof(uint64_t));
-	PP_AL(w_.lb_act, (size_t) tiles * sizeof(uint64_t));
+	PP_AL(w_.lb_fin, ((size_t) tiles + 1) * sizeof(uint64_t));
 	PP_AL(w_.ctr, sizeof(WorldCounters));
 	PP_AL(w_.hist, 8 * 256 * 4);
 	PP_AL(w_.ring, (size_t) w_.ring_rows * nruns_cap * sizeof(PPStatistics));
 #undef PP_AL
 	PP_CK(cudaMemsetAsync(w_.lb_sort, 0, sort_tiles * 256 * sizeof(uint64_t), s_));
-	PP_CK(cudaMemsetAsync(w_.lb_act, 0, (size_t) tiles * sizeof(uint64_t), s_));
+	PP_CK(cudaMemsetAsync(w_.lb_fin, 0, ((size_t) tiles + 1) * sizeof(uint64_t), s_));
+	PP_CK(cudaMemsetAsync(w_.rcnt, 0, (size_t) tiles * 4, s_));
+	PP_CK(cudaMemsetAsync(w_.rstart, 0, (size_t) tiles * 4, s_));
 	PP_CK(cudaMemsetAsync(w_.hist, 0, 8 * 256 * 4, s_));
 	PP_CK(cudaMemsetAsync(w_.ring, 0, (size_t) w_.ring_rows * nruns_cap * sizeof(PPStatistics), s_));
 	PP_CK(cudaMemsetAsync(w_.part, 0, (size_t) tiles * 8 * sizeof(uint64_t), s_));
@@ -224,18 +230,19 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	/* Launch geometry. */
 	lc_.sms = sms;
 	lc_.cpt = (int) (T / ACT_THREADS);
-	size_t act_smem = (size_t) act_cap * 16;
+	size_t act_smem = (size_t) act_cap * 16 + (size_t) T * 2;
 	PP_CK(set_act_smem_limits(act_smem));
 	int occ_sort = occupancy_sort((int) d);
 	if (occ_sort < 1) occ_sort = 1;
 	lc_.sort_blocks = sms * occ_sort;
-	lc_.move_blocks = sms * 8;
+	lc_.move_blocks = (int) std::max<uint64_t>(1, std::min<uint64_t>((tiles + 7) / 8, (uint64_t) sms * 8));
 	lc_.offs_blocks = sms * 8;
 	lc_.finish_blocks = (int) std::min<uint64_t>(tiles, (uint64_t) sms * 2);
 
 	/* Initial state: grass, then every run's agents in creation order into
-	 * B at the run's base, sorted by cell into A (runs occupy increasing
-	 * cell ranges, so each run's agents stay at its base), stats row 0. */
+	 * B at the run's base, sorted by cell into the region buffer (runs
+	 * occupy increasing cell ranges, so each run's agents stay at its
+	 * base), the tiles' regions and dense bases, stats row 0. */
 	for (size_t r = 0; r < runs.size(); r++) {
 		rc = cuda_status(enqueue_init_grass(w_, runs_h_[r], s_));
 		if (rc) return rc;
@@ -243,13 +250,13 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 			runs[r].p.init_sheep, runs[r].p.init_wolves, s_));
 		if (rc) return rc;
 	}
-	rc = sort_into(base, w_.kA, w_.vA);
+	rc = sort_into(base, w_.kR, w_.vR);
 	if (rc) return rc;
-	PP_CK(cudaMemcpyAsync(&w_.ctr->n_agents, &base, 4, cudaMemcpyHostToDevice, s_));
-	h2d_ += 4;
+	rc = cuda_status(enqueue_regions_from_sorted(w_, lc_, w_.kR, 0, (uint32_t) tiles, 0, s_));
+	if (rc) return rc;
 	for (size_t r = 0; r < runs.size(); r++) {
-		rc = cuda_status(enqueue_stats_run(w_, runs_h_[r], (uint32_t) r, base_h[r],
-			runs[r].p.init_sheep + runs[r].p.init_wolves, 0, s_));
+		rc = cuda_status(enqueue_stats_run(w_, runs_h_[r], (uint32_t) r,
+			w_.vR + base_h[r], runs[r].p.init_sheep + runs[r].p.init_wolves, 0, s_));
 		if (rc) return rc;
 	}
 	giter_ = 0;
@@ -317,7 +324,10 @@ int World::enqueue(uint32_t n)
 	}
 	for (; done < n; done++) PP_CK(enqueue_iteration(w_, lc_, s_));
 	giter_ += n;
-	if (n) release_pending();
+	if (n) {
+		release_pending();
+		adm_used_ = 0;   /* the act rewrote every region below 2 * cap */
+	}
 	return PP_SUCCESS;
 }
 
@@ -371,6 +381,8 @@ int World::get_state(uint32_t *cell, uint32_t *en, uint32_t n_max,
 	PP_CK(cudaMemcpy(&n, &w_.ctr->n_agents, 4, cudaMemcpyDeviceToHost));
 	if (n_out) *n_out = n;
 	uint32_t m = std::min(n, n_max);
+	PP_CK(enqueue_compact(w_, lc_, w_.kA, w_.vA, s_));
+	PP_CK(cudaStreamSynchronize(s_));
 	if (cell && m) PP_CK(cudaMemcpy(cell, w_.kA, (size_t) m * 4, cudaMemcpyDeviceToHost));
 	if (en && m) PP_CK(cudaMemcpy(en, w_.vA, (size_t) m * 4, cudaMemcpyDeviceToHost));
 	if (grass) {
@@ -471,7 +483,7 @@ int World::admit(const RunSpec &spec, uint32_t *slot_out)
 	uint32_t n = 0;
 	PP_CK(cudaMemcpy(&n, &w_.ctr->n_agents, 4, cudaMemcpyDeviceToHost));
 	uint32_t n0 = spec.p.init_sheep + spec.p.init_wolves;
-	if ((uint64_t) n + n0 > w_.cap) {
+	if ((uint64_t) n + n0 > w_.cap || (uint64_t) adm_used_ + n0 > w_.cap) {
 		free_tiles_.push_back({first, need});
 		return PP_OUT_OF_RESOURCES;
 	}
@@ -489,13 +501,17 @@ int World::admit(const RunSpec &spec, uint32_t *slot_out)
 	rc = cuda_status(enqueue_init_agents(run, w_.kB, w_.vB, 0,
 		spec.p.init_sheep, spec.p.init_wolves, s_));
 	if (rc) return rc;
-	rc = sort_into(n0, w_.kA + n, w_.vA + n);
+	/* The agents go to the admission area of the region buffer (after the
+	 * 2 * cap slots the act writes), as the regions of the run's tiles. */
+	const uint32_t adm = 2 * w_.cap + adm_used_;
+	rc = sort_into(n0, w_.kR + adm, w_.vR + adm);
 	if (rc) return rc;
-	rc = cuda_status(enqueue_stats_run(w_, run, slot, n, n0, row, s_));
+	rc = cuda_status(enqueue_regions_from_sorted(w_, lc_, w_.kR + adm, first, need, adm, s_));
 	if (rc) return rc;
-	uint32_t nn = n + n0;
-	PP_CK(cudaMemcpyAsync(&w_.ctr->n_agents, &nn, 4, cudaMemcpyHostToDevice, s_));
-	h2d_ += sizeof(RunDev) + need * 2 + 4;
+	adm_used_ += n0;
+	rc = cuda_status(enqueue_stats_run(w_, run, slot, w_.vR + adm, n0, row, s_));
+	if (rc) return rc;
+	h2d_ += sizeof(RunDev) + need * 2;
 	d2h_ += 4;
 	*slot_out = slot;
 	return PP_SUCCESS;

@@ -101,6 +101,7 @@ private:
 	std::vector<std::pair<std::pair<uint32_t, uint32_t>, uint32_t>> pending_tiles_;
 	void release_pending();
 	uint32_t agents_reserved_ = 0;
+	uint32_t adm_used_ = 0;   /* admission area of the region buffer in use */
 public:
 	uint64_t h2d_ = 0, d2h_ = 0;   /* bytes copied host<->device by the world */
 private:
