@@ -193,26 +193,30 @@ __global__ void k_offsets(const uint32_t *keys, const uint32_t *n_dev,
 /* Act                                                                 */
 /* ------------------------------------------------------------------ */
 
-/* Actions of the agents of one cell (local index lc), entries [p, e) of
- * the tile's agent list in cell-list order, in increasing (priority, rank)
- * order; priority and dice of the agent of rank k come from
- * Philox({lc, t, ACT, k}). This is the sequential semantics of
- * pp_cpu.cl:640-848 (wolves eat the first not-yet-eaten sheep of the cell;
- * a sheep acts only if not eaten before its turn; the first acting sheep
- * takes live grass; every acting agent may reproduce) in closed form: the
- * k-th wolf eats the k-th sheep, and a sheep acts iff the wolves before it
- * are no more than the sheep before it.
+/* Model parameters the actions need, held in registers. */
+struct ActParams {
+	uint32_t sheep_gain, sheep_thr, sheep_prob;
+	uint32_t wolves_gain, wolves_thr, wolves_prob;
+	uint32_t restart;
+};
+
+/* Actions of the agents of one cell, entries [p, e) of the tile's agent
+ * list in cell-list order, in increasing (priority, rank) order; on entry
+ * LP[j] / LD[j] hold the priority and the dice of the agent of rank j - p,
+ * drawn from Philox({cell, t, ACT, rank}). This is the sequential semantics
+ * of pp_cpu.cl:640-848 (wolves eat the first not-yet-eaten sheep of the
+ * cell; a sheep acts only if not eaten before its turn; the first acting
+ * sheep takes live grass; every acting agent may reproduce) in closed form:
+ * the k-th wolf eats the k-th sheep, and a sheep acts iff the wolves before
+ * it are no more than the sheep before it.
  * On return LV[j] holds type | final energy (energy 0 = eaten) and LD[j]
  * the newborn's energy (0 = none). */
-__device__ __noinline__ void act_cell(uint32_t p, uint32_t e,
-	uint32_t *LV, uint32_t *LP, uint32_t *LD, const RunDev &run,
-	uint32_t lc, uint32_t t, uint32_t &g)
+__device__ __forceinline__ void act_cell(uint32_t p, uint32_t e,
+	uint32_t *LV, const uint32_t *LP, uint32_t *LD, const ActParams &ap,
+	uint32_t &g)
 {
 	uint32_t S = 0, W = 0;
 	for (uint32_t j = p; j < e; j++) {
-		u4 r = rng(run.seed_lo, run.seed_hi, lc, t, STREAM_ACT, j - p);
-		LP[j] = r.x;
-		LD[j] = draw(r.y, 100);
 		if (LV[j] & TYPE_BIT) W++;
 		else S++;
 	}
@@ -242,21 +246,21 @@ __device__ __noinline__ void act_cell(uint32_t p, uint32_t e,
 		bool acts, eaten = false;
 		uint32_t thr, prob;
 		if (tb) {
-			if (wb < S) en += run.wolves_gain;
+			if (wb < S) en += ap.wolves_gain;
 			wb++;
 			acts = true;
-			thr = run.wolves_thr;
-			prob = run.wolves_prob;
+			thr = ap.wolves_thr;
+			prob = ap.wolves_prob;
 		} else {
 			acts = wb <= sb;
 			eaten = sb < W;
 			sb++;
 			if (acts && g == 0) {
-				g = run.restart;
-				en += run.sheep_gain;
+				g = ap.restart;
+				en += ap.sheep_gain;
 			}
-			thr = run.sheep_thr;
-			prob = run.sheep_prob;
+			thr = ap.sheep_thr;
+			prob = ap.sheep_prob;
 		}
 		uint32_t kid = 0;
 		if (acts && en > thr && dice < prob) {
@@ -410,9 +414,15 @@ __device__ __forceinline__ void store_grass(uint16_t *gp, const uint16_t *gr)
 	}
 }
 
-/* One CTA per tile of CPT * 256 cells; tiles are taken by ticket so a
- * tile's predecessors are always running or done (the look-back cannot
- * wait on a CTA that is not resident). */
+/* One CTA per tile of CPT * 256 cells, taken by ticket. Phases:
+ *   A (per cell)  grass countdown into shared memory, cells transposed
+ *                 across threads so the 16-bit accesses do not conflict;
+ *   B (per agent) priority and dice of every agent (its rank = distance
+ *                 to its cell's first entry);
+ *   C (per cell with agents, from its first agent) the cell's actions;
+ *   D (per cell)  grass stats and vector store;
+ *   E (per agent chunk) survivors and newborns, in list order, into the
+ *                 tile's region [2 * a0, 2 * a0 + total), agent stats. */
 template <int CPT>
 __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	const uint32_t *__restrict__ kS, uint32_t *__restrict__ vS)
@@ -420,6 +430,7 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	extern __shared__ uint32_t sm[];
 	uint32_t *sk = sm, *sv = sm + w.act_cap, *sp = sv + w.act_cap,
 		*sd = sp + w.act_cap;
+	uint16_t *sg = reinterpret_cast<uint16_t *>(sd + w.act_cap);
 	__shared__ uint32_t s_tile;
 	__shared__ uint64_t s_part[6];
 	const uint32_t tid = threadIdx.x;
@@ -428,11 +439,9 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	const uint32_t tile = s_tile;
 	if (tile >= w.n_tiles) return;
 	const uint32_t g = w.ctr->giter + 1;
-	const uint32_t r = w.tile_run[tile];
-	const RunDev run = w.runs[r];
+	const RunDev &run = w.runs[w.tile_run[tile]];
 	const uint32_t t = g - run.start_giter;
-	const bool live = run_live(run, t);
-	if (!live) {
+	if (!run_live(run, t)) {
 		/* finished run or free tile space: no agents survive, no stats */
 		if (tid == 0) {
 			w.rstart[tile] = 0;
@@ -441,11 +450,15 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 		if (tid < 8) w.part[(size_t) tile * 8 + tid] = 0;
 		return;
 	}
+	const uint32_t seed_lo = run.seed_lo, seed_hi = run.seed_hi;
+	const uint32_t cbase = run.cbase, ncells = run.ncells;
+	ActParams ap;
+	ap.sheep_gain = run.sheep_gain; ap.sheep_thr = run.sheep_thr;
+	ap.sheep_prob = run.sheep_prob; ap.wolves_gain = run.wolves_gain;
+	ap.wolves_thr = run.wolves_thr; ap.wolves_prob = run.wolves_prob;
+	ap.restart = run.restart;
 	const uint32_t c0 = tile << w.log_tile;
-	const uint32_t cell0 = tid * CPT;
-	uint16_t gr[CPT];
-	uint16_t *gp = w.grass + c0 + cell0;
-	load_grass<CPT>(gp, gr);
+	const uint32_t lt0 = c0 - cbase;          /* run-local index of the tile start */
 	const uint32_t a0 = w.tile_off[tile], a1 = w.tile_off[tile + 1];
 	const uint32_t m = a1 - a0;
 	const bool in_smem = m <= w.act_cap;
@@ -453,59 +466,68 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	if (in_smem) {
 		LK = sk; LV = sv; LP = sp; LD = sd;
 		for (uint32_t j = tid; j < m; j += ACT_THREADS) {
-			sk[j] = kS[a0 + j];
+			sk[j] = kS[a0 + j] - c0;
 			sv[j] = vS[a0 + j];
 		}
 	} else {
-		LK = const_cast<uint32_t *>(kS) + a0;
+		LK = w.scratch_key + a0;
 		LV = vS + a0;
 		LP = w.scratch_prio + a0;
 		LD = w.scratch_kid + a0;
+		for (uint32_t j = tid; j < m; j += ACT_THREADS) LK[j] = kS[a0 + j] - c0;
 	}
-	__syncthreads();
-	StatAcc acc;
-	acc.zero();
-	const uint32_t lc0 = c0 - run.cbase + cell0;
-	/* Countdown of this thread's cells into its slice of shared memory
-	 * (cells past the run's grid are padding and stay untouched). */
-	uint16_t *sg = reinterpret_cast<uint16_t *>(sd + w.act_cap) + cell0;
+	/* A: countdown (cells past the run's grid are padding, untouched) */
+	const uint32_t cell0 = tid * CPT;
+	uint16_t gr[CPT];
+	uint16_t *gp = w.grass + c0 + cell0;
+	load_grass<CPT>(gp, gr);
 #pragma unroll
 	for (int q = 0; q < CPT; q++) {
 		uint32_t gq = gr[q];
-		if (gq > 0 && (lc0 + q) < run.ncells) gq--;
-		sg[q] = (uint16_t) gq;
+		if (gq > 0 && (lt0 + cell0 + q) < ncells) gq--;
+		sg[q * ACT_THREADS + tid] = (uint16_t) gq;
 	}
-	const uint32_t pbeg = lower_bound_u32(LK, m, c0 + cell0);
-	const uint32_t pend = lower_bound_u32(LK, m, c0 + cell0 + CPT);
-	/* Actions, occupied cells only. */
-	for (uint32_t p = pbeg; p < pend;) {
-		const uint32_t cell = LK[p];
-		uint32_t e = p + 1;
-		while (e < pend && LK[e] == cell) e++;
-		const uint32_t q = cell - (c0 + cell0);
-		uint32_t gq = sg[q];
-		act_cell(p, e, LV, LP, LD, run, lc0 + q, t, gq);
-		sg[q] = (uint16_t) gq;
-		p = e;
+	__syncthreads();
+	/* B: draws of every agent */
+	for (uint32_t j = tid; j < m; j += ACT_THREADS) {
+		const uint32_t lc = LK[j];
+		uint32_t k = 0;
+		while (k < j && LK[j - k - 1] == lc) k++;
+		u4 r = rng(seed_lo, seed_hi, lt0 + lc, t, STREAM_ACT, k);
+		LP[j] = r.x;
+		LD[j] = draw(r.y, 100);
 	}
+	__syncthreads();
+	/* C: actions, one thread per occupied cell (its first agent's) */
+	for (uint32_t j = tid; j < m; j += ACT_THREADS) {
+		const uint32_t lc = LK[j];
+		if (j > 0 && LK[j - 1] == lc) continue;
+		uint32_t e = j + 1;
+		while (e < m && LK[e] == lc) e++;
+		uint16_t *gs = &sg[(lc % CPT) * ACT_THREADS + lc / CPT];
+		uint32_t gq = *gs;
+		act_cell(j, e, LV, LP, LD, ap, gq);
+		*gs = (uint16_t) gq;
+	}
+	__syncthreads();
+	/* D: grass stats and store */
+	uint32_t galive = 0, gsum = 0;
 #pragma unroll
 	for (int q = 0; q < CPT; q++) {
-		const uint32_t gq = sg[q];
-		if ((lc0 + q) < run.ncells) {
-			acc.galive += gq == 0;
-			acc.gen += gq;
+		const uint32_t gq = sg[q * ACT_THREADS + tid];
+		if ((lt0 + cell0 + q) < ncells) {
+			galive += gq == 0;
+			gsum += gq;
 		}
 		gr[q] = (uint16_t) gq;
 	}
 	store_grass<CPT>(gp, gr);
-	/* Survivors + newborns of this thread, in list order. */
+	/* E: outputs in list order, contiguous agent chunks per thread */
+	const uint32_t ch = (m + ACT_THREADS - 1) / ACT_THREADS;
+	const uint32_t ja = min(tid * ch, m), jb = min(ja + ch, m);
 	uint32_t cnt = 0;
-	for (uint32_t j = pbeg; j < pend; j++)
+	for (uint32_t j = ja; j < jb; j++)
 		cnt += ((LV[j] & ENERGY_MASK) != 0) + (LD[j] != 0);
-	/* The tile's next lists go to its own region of the region buffer,
-	 * [2 * a0, 2 * a0 + total): at most two outputs per input agent, so
-	 * regions never overlap and no tile waits for another. The dense
-	 * position of each region comes from the scan in k_finish. */
 	uint32_t total;
 	const uint32_t excl = block_excl_scan(cnt, &total);
 	const uint32_t rs = 2 * a0;
@@ -514,24 +536,30 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 		w.rcnt[tile] = total;
 	}
 	uint32_t o = rs + excl;
-	for (uint32_t j = pbeg; j < pend; j++) {
-		const uint32_t v = LV[j], k = LK[j], kd = LD[j];
+	uint32_t sheep = 0, wolves = 0;
+	uint64_t sen = 0, wen = 0;
+	for (uint32_t j = ja; j < jb; j++) {
+		const uint32_t v = LV[j], k = LK[j] + c0, kd = LD[j];
 		const uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
 		if (en) {
 			w.kR[o] = k;
 			w.vR[o] = v;
 			o++;
-			if (tb) { acc.wolves++; acc.wen += en; }
-			else { acc.sheep++; acc.sen += en; }
+			if (tb) { wolves++; wen += en; }
+			else { sheep++; sen += en; }
 		}
 		if (kd) {
 			w.kR[o] = k;
 			w.vR[o] = tb | kd;
 			o++;
-			if (tb) { acc.wolves++; acc.wen += kd; }
-			else { acc.sheep++; acc.sen += kd; }
+			if (tb) { wolves++; wen += kd; }
+			else { sheep++; sen += kd; }
 		}
 	}
+	/* per-tile partial stats */
+	StatAcc acc;
+	acc.sheep = sheep; acc.wolves = wolves; acc.galive = galive;
+	acc.sen = sen; acc.wen = wen; acc.gen = gsum;
 	block_stats(acc, s_part);
 	if (tid < 6) w.part[(size_t) tile * 8 + tid] = s_part[tid];
 }
@@ -762,6 +790,8 @@ cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
 	if (marks) cudaEventRecord(marks[2 + w.passes], s);
 	size_t act_smem = (size_t) w.act_cap * 4 * sizeof(uint32_t)
 		+ ((size_t) lc.cpt * ACT_THREADS) * sizeof(uint16_t);
+	/* (the shared-memory layout of k_act: keys, values, priorities,
+	 * dice/newborns, then the tile's countdowns) */
 	switch (lc.cpt) {
 	case 4: k_act<4><<<w.n_tiles, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
 	case 16: k_act<16><<<w.n_tiles, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;

@@ -185,6 +185,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	PP_AL(w_.kB, cap * 4); PP_AL(w_.vB, cap * 4);
 	PP_AL(w_.kC, cap * 4); PP_AL(w_.vC, cap * 4);
 	PP_AL(w_.kR, 3 * cap * 4); PP_AL(w_.vR, 3 * cap * 4);
+	PP_AL(w_.scratch_key, cap * 4);
 	PP_AL(w_.scratch_prio, cap * 4); PP_AL(w_.scratch_kid, cap * 4);
 	PP_AL(w_.rstart, (size_t) tiles * 4);
 	PP_AL(w_.rcnt, (size_t) tiles * 4);
