@@ -82,6 +82,55 @@ __device__ __forceinline__ uint32_t lookback(uint64_t *lb, size_t stride,
 	return acc;
 }
 
+/* The same look-back with four predecessor words in flight per step: the
+ * walk over predecessors that have published only their aggregate costs a
+ * quarter of the round trips. */
+__device__ __forceinline__ uint32_t lookback4(uint64_t *lb, size_t stride,
+	uint32_t tile, uint32_t agg, uint32_t epoch, uint32_t *err)
+{
+	if (tile == 0) {
+		st_release_u64(&lb[0], lb_pack(epoch, LB_FLAG_PREFIX, agg));
+		return 0;
+	}
+	st_release_u64(&lb[(size_t) tile * stride],
+		lb_pack(epoch, LB_FLAG_AGG, agg));
+	const uint32_t ep = epoch & 0x3fffffffu;
+	uint32_t acc = 0;
+	int64_t k = (int64_t) tile - 1;
+	uint32_t spins = 0;
+	while (k >= 0) {
+		uint64_t wv[4];
+#pragma unroll
+		for (int q = 0; q < 4; q++)
+			wv[q] = (k - q >= 0) ? ld_acquire_u64(&lb[(size_t) (k - q) * stride]) : 0;
+		bool done = false;
+		int used = 0;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			if (done || used != q) break;
+			if (k - q < 0) { done = true; break; }
+			uint32_t wep = (uint32_t) (wv[q] >> 34);
+			uint32_t flag = (uint32_t) (wv[q] >> 32) & 3u;
+			if (wep != ep || flag == 0) break;   /* not yet published */
+			acc += (uint32_t) wv[q];
+			used++;
+			if (flag == LB_FLAG_PREFIX) done = true;
+		}
+		if (done) break;
+		k -= used;
+		if (used == 0) {
+			if (++spins > SPIN_LIMIT) {
+				atomicOr(err, ERRF_TIMEOUT);
+				break;
+			}
+			if (spins > 32) __nanosleep(64);
+		}
+	}
+	st_release_u64(&lb[(size_t) tile * stride],
+		lb_pack(epoch, LB_FLAG_PREFIX, acc + agg));
+	return acc;
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v)
 {

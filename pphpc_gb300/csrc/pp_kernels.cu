@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(256) k_regions(WorldDev w, uint32_t *ko,
 			 * one per lane. */
 			const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
 			for (uint32_t p = 0; p < P; p++) {
-				uint32_t dig = (nk >> (p * d)) & mask;
+				uint32_t dig = (nk >> (w.sort_shift + p * d)) & mask;
 				uint32_t d0 = __shfl_sync(0xffffffffu, dig, 0);
 				bool same = __all_sync(0xffffffffu, !valid || dig == d0);
 				if (same) {
@@ -415,6 +415,9 @@ __device__ __forceinline__ void store_grass(uint16_t *gp, const uint16_t *gr)
 }
 
 /* One CTA per tile of CPT * 256 cells, taken by ticket. Phases:
+ *   (grouping)    the tile's agents arrive grouped by tile in canonical
+ *                 order; a counting sort by cell in shared memory, each
+ *                 cell's short list put back in arrival order;
  *   A (per cell)  grass countdown into shared memory, cells transposed
  *                 across threads so the 16-bit accesses do not conflict;
  *   B (per agent) priority and dice of every agent (its rank = distance
@@ -429,8 +432,9 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 {
 	extern __shared__ uint32_t sm[];
 	uint32_t *sk = sm, *sv = sm + w.act_cap, *sp = sv + w.act_cap,
-		*sd = sp + w.act_cap;
-	uint16_t *sg = reinterpret_cast<uint16_t *>(sd + w.act_cap);
+		*sd = sp + w.act_cap, *sperm = sd + w.act_cap;
+	uint32_t *scnt = sperm + w.act_cap;                 /* CPT * 256 */
+	uint16_t *sg = reinterpret_cast<uint16_t *>(scnt + CPT * ACT_THREADS);
 	__shared__ uint32_t s_tile;
 	__shared__ uint64_t s_part[6];
 	const uint32_t tid = threadIdx.x;
@@ -462,22 +466,29 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	const uint32_t a0 = w.tile_off[tile], a1 = w.tile_off[tile + 1];
 	const uint32_t m = a1 - a0;
 	const bool in_smem = m <= w.act_cap;
-	uint32_t *LK, *LV, *LP, *LD;
+	/* The sort grouped agents by tile only, in canonical order (source
+	 * cell, source rank); group them by cell here, keeping that order. */
+	uint32_t *UK, *UV, *PERM, *LK, *LV, *LP, *LD;
 	if (in_smem) {
-		LK = sk; LV = sv; LP = sp; LD = sd;
+		UK = sk; UV = sv; PERM = sperm; LK = sp; LV = sd; LP = sk; LD = sv;
 		for (uint32_t j = tid; j < m; j += ACT_THREADS) {
-			sk[j] = kS[a0 + j] - c0;
+			sk[j] = kS[a0 + j];
 			sv[j] = vS[a0 + j];
 		}
 	} else {
-		LK = w.scratch_key + a0;
-		LV = vS + a0;
-		LP = w.scratch_prio + a0;
-		LD = w.scratch_kid + a0;
-		for (uint32_t j = tid; j < m; j += ACT_THREADS) LK[j] = kS[a0 + j] - c0;
+		UK = const_cast<uint32_t *>(kS) + a0; UV = vS + a0;
+		PERM = w.scratch_perm + a0;
+		LK = w.scratch_key + a0; LV = w.scratch_val + a0;
+		LP = w.scratch_prio + a0; LD = w.scratch_kid + a0;
 	}
-	/* A: countdown (cells past the run's grid are padding, untouched) */
 	const uint32_t cell0 = tid * CPT;
+	/* per-cell counters, transposed like the countdowns: cell c lives at
+	 * SLOT(c) = (c % CPT) * 256 + c / CPT, so no two threads of a warp
+	 * share a bank */
+#define SLOT(c) ((((c) % CPT) * ACT_THREADS) + (c) / CPT)
+#pragma unroll
+	for (int q = 0; q < CPT; q++) scnt[q * ACT_THREADS + tid] = 0;
+	/* A: countdown (cells past the run's grid are padding, untouched) */
 	uint16_t gr[CPT];
 	uint16_t *gp = w.grass + c0 + cell0;
 	load_grass<CPT>(gp, gr);
@@ -486,6 +497,55 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 		uint32_t gq = gr[q];
 		if (gq > 0 && (lt0 + cell0 + q) < ncells) gq--;
 		sg[q * ACT_THREADS + tid] = (uint16_t) gq;
+	}
+	__syncthreads();
+	/* counting sort of the tile's agents by cell */
+	for (uint32_t j = tid; j < m; j += ACT_THREADS) {
+		const uint32_t lc = UK[j] - c0;
+		atomicAdd(&scnt[SLOT(lc)], 1u);
+	}
+	__syncthreads();
+	{
+		uint32_t loc = 0;
+#pragma unroll
+		for (int q = 0; q < CPT; q++) loc += scnt[q * ACT_THREADS + tid];
+		uint32_t tot;
+		uint32_t run_start = block_excl_scan(loc, &tot);
+#pragma unroll
+		for (int q = 0; q < CPT; q++) {
+			uint32_t c = scnt[q * ACT_THREADS + tid];
+			scnt[q * ACT_THREADS + tid] = run_start;
+			run_start += c;
+		}
+	}
+	__syncthreads();
+	for (uint32_t j = tid; j < m; j += ACT_THREADS) {
+		const uint32_t lc = UK[j] - c0;
+		PERM[atomicAdd(&scnt[SLOT(lc)], 1u)] = j;
+	}
+	__syncthreads();
+	/* scnt[SLOT(c)] is now the end of cell c; restore the arrival order of
+	 * each cell's (short) list */
+	{
+		uint32_t b = tid ? scnt[(CPT - 1) * ACT_THREADS + tid - 1] : 0;
+#pragma unroll 1
+		for (int q = 0; q < CPT; q++) {
+			const uint32_t e = scnt[q * ACT_THREADS + tid];
+			for (uint32_t i = b + 1; i < e; i++) {
+				const uint32_t x = PERM[i];
+				uint32_t h = i;
+				while (h > b && PERM[h - 1] > x) { PERM[h] = PERM[h - 1]; h--; }
+				PERM[h] = x;
+			}
+			b = e;
+		}
+	}
+#undef SLOT
+	__syncthreads();
+	for (uint32_t i = tid; i < m; i += ACT_THREADS) {
+		const uint32_t j = PERM[i];
+		LK[i] = UK[j] - c0;
+		LV[i] = UV[j];
 	}
 	__syncthreads();
 	/* B: draws of every agent */
@@ -777,7 +837,7 @@ cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
 	uint32_t *ki = w.kB, *vi = w.vB, *ko = w.kC, *vo = w.vC;
 	for (uint32_t p = 0; p < w.passes; p++) {
 		cudaError_t e = launch_radix_pass(ki, vi, ko, vo, w.hist + p * 256,
-			w.lb_sort, w.ctr, &w.ctr->n_agents, p, p * w.digit_bits,
+			w.lb_sort, w.ctr, &w.ctr->n_agents, p, w.sort_shift + p * w.digit_bits,
 			w.digit_bits, lc.sort_blocks, s);
 		if (e != cudaSuccess) return e;
 		if (marks) cudaEventRecord(marks[2 + p], s);
@@ -788,10 +848,10 @@ cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
 	k_offsets<<<lc.offs_blocks, 256, 0, s>>>(ki, &w.ctr->n_agents,
 		w.log_tile, w.n_tiles, w.tile_off);
 	if (marks) cudaEventRecord(marks[2 + w.passes], s);
-	size_t act_smem = (size_t) w.act_cap * 4 * sizeof(uint32_t)
-		+ ((size_t) lc.cpt * ACT_THREADS) * sizeof(uint16_t);
-	/* (the shared-memory layout of k_act: keys, values, priorities,
-	 * dice/newborns, then the tile's countdowns) */
+	size_t act_smem = (size_t) w.act_cap * 5 * sizeof(uint32_t)
+		+ ((size_t) lc.cpt * ACT_THREADS) * (sizeof(uint32_t) + sizeof(uint16_t));
+	/* (the shared-memory layout of k_act: five agent arrays, then per-cell
+	 * counters and countdowns of the tile) */
 	switch (lc.cpt) {
 	case 4: k_act<4><<<w.n_tiles, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
 	case 16: k_act<16><<<w.n_tiles, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;

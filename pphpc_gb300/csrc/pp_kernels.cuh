@@ -29,10 +29,12 @@ struct WorldDev {
 	WorldCounters *ctr;
 	uint32_t *hist;           /* [8][256] digit counts of the moved keys   */
 	PPStatistics *ring;       /* [ring_rows][nruns_cap]                    */
-	uint32_t *scratch_key, *scratch_prio, *scratch_kid; /* [cap], act fallback */
+	uint32_t *scratch_key, *scratch_val, *scratch_prio, *scratch_kid,
+		*scratch_perm;        /* [cap], act fallback for crowded tiles     */
 	uint64_t *part;           /* [n_tiles][8] per-tile partial stats       */
 	uint32_t cap, n_tiles, log_tile, nruns_cap, ring_rows;
 	uint32_t key_bits, digit_bits, passes;
+	uint32_t sort_shift;      /* the sort orders key bits [sort_shift, key_bits) */
 	uint32_t act_cap;         /* agents per tile held in shared memory     */
 	uint32_t dead_key;        /* = n_tiles << log_tile                      */
 };

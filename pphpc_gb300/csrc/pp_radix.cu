@@ -58,7 +58,7 @@ __device__ __forceinline__ uint32_t lanemask_lt()
 }
 
 template <int DBITS>
-__global__ void __launch_bounds__(SORT_THREADS) k_radix_pass(
+__global__ void __launch_bounds__(SORT_THREADS, 3) k_radix_pass(
 	const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
 	uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
 	const uint32_t *__restrict__ hist_pass, uint64_t *lb, WorldCounters *ctr,
@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_pass(
 		uint32_t tstart = block_excl_scan(cnt, &tot);
 		if (tid < RADIX) {
 			s_tile_start[tid] = tstart;
-			uint32_t ex = lookback(lb + tid, RADIX, tile, cnt, epoch,
+			uint32_t ex = lookback4(lb + tid, RADIX, tile, cnt, epoch,
 				&ctr->err);
 			s_gpos[tid] = s_digit_base[tid] + ex;
 		}

@@ -156,22 +156,26 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	w_.dead_key = (uint32_t) (tiles << log_tile);
 	uint32_t kb = 32 - __builtin_clz(w_.dead_key);
 	w_.key_bits = kb;
+	/* The act groups a tile's agents by cell itself, so the sort orders
+	 * only the tile bits of the cell key. */
+	w_.sort_shift = log_tile;
+	const uint32_t sb = kb > log_tile ? kb - log_tile : 1;
 	uint32_t d = cfg.digit_bits;
 	if (d == 0) {
-		uint32_t passes = (kb + 7) / 8;
-		d = (kb + passes - 1) / passes;
+		uint32_t passes = (sb + 7) / 8;
+		d = (sb + passes - 1) / passes;
 	}
 	if (d < 5) d = 5;
 	if (d > 8) return PP_INVALID_ARGS;
 	w_.digit_bits = d;
-	w_.passes = (kb + d - 1) / d;
+	w_.passes = (sb + d - 1) / d;
 	if (w_.passes > 8) return PP_INVALID_ARGS;
 
 	uint32_t act_cap = cfg.act_cap;
 	if (act_cap == 0) {
 		double dens = total_cells ? (double) cfg.cap / (double) total_cells : 2.0;
 		if (dens > 2.0) dens = 2.0;
-		act_cap = pow2_ceil((uint32_t) (T * dens * 1.5) + 1);
+		act_cap = pow2_ceil((uint32_t) (T * dens * 0.75) + 1);
 		act_cap = std::min<uint32_t>(std::max<uint32_t>(act_cap, 256), 4096);
 	}
 	w_.act_cap = act_cap;
@@ -185,8 +189,9 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	PP_AL(w_.kB, cap * 4); PP_AL(w_.vB, cap * 4);
 	PP_AL(w_.kC, cap * 4); PP_AL(w_.vC, cap * 4);
 	PP_AL(w_.kR, 3 * cap * 4); PP_AL(w_.vR, 3 * cap * 4);
-	PP_AL(w_.scratch_key, cap * 4);
+	PP_AL(w_.scratch_key, cap * 4); PP_AL(w_.scratch_val, cap * 4);
 	PP_AL(w_.scratch_prio, cap * 4); PP_AL(w_.scratch_kid, cap * 4);
+	PP_AL(w_.scratch_perm, cap * 4);
 	PP_AL(w_.rstart, (size_t) tiles * 4);
 	PP_AL(w_.rcnt, (size_t) tiles * 4);
 	PP_AL(w_.dbase, ((size_t) tiles + 1) * 4);
@@ -231,7 +236,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	/* Launch geometry. */
 	lc_.sms = sms;
 	lc_.cpt = (int) (T / ACT_THREADS);
-	size_t act_smem = (size_t) act_cap * 16 + (size_t) T * 2;
+	size_t act_smem = (size_t) act_cap * 20 + (size_t) T * 6;
 	PP_CK(set_act_smem_limits(act_smem));
 	int occ_sort = occupancy_sort((int) d);
 	if (occ_sort < 1) occ_sort = 1;
@@ -272,18 +277,22 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 
 int World::sort_into(uint32_t n, uint32_t *dst_k, uint32_t *dst_v)
 {
-	/* Stable radix sort of B[0, n) by cell on the world's counters, then a
-	 * copy to dst; leaves fresh epochs, tickets and histograms. */
+	/* Stable radix sort of B[0, n) by the whole cell key (every region is a
+	 * run of cell-sorted lists) on the world's counters, then a copy to
+	 * dst; leaves fresh epochs, tickets and histograms. */
 	PP_CK(cudaMemcpyAsync(&w_.ctr->aux_n, &n, 4, cudaMemcpyHostToDevice, s_));
 	h2d_ += 4;
 	if (n) {
-		PP_CK(launch_radix_hist(w_.kB, &w_.ctr->aux_n, w_.hist, w_.digit_bits,
-			w_.passes, lc_.move_blocks, s_));
+		const uint32_t kb = w_.key_bits;
+		const uint32_t passes = (kb + 7) / 8;
+		uint32_t d = (kb + passes - 1) / passes;
+		if (d < 5) d = 5;
+		PP_CK(launch_radix_hist(w_.kB, &w_.ctr->aux_n, w_.hist, d, passes,
+			lc_.move_blocks, s_));
 		uint32_t *ki = w_.kB, *vi = w_.vB, *ko = w_.kC, *vo = w_.vC;
-		for (uint32_t p = 0; p < w_.passes; p++) {
+		for (uint32_t p = 0; p < passes; p++) {
 			PP_CK(launch_radix_pass(ki, vi, ko, vo, w_.hist + p * 256, w_.lb_sort,
-				w_.ctr, &w_.ctr->aux_n, p, p * w_.digit_bits, w_.digit_bits,
-				lc_.sort_blocks, s_));
+				w_.ctr, &w_.ctr->aux_n, p, p * d, d, lc_.sort_blocks, s_));
 			std::swap(ki, ko);
 			std::swap(vi, vo);
 		}
