@@ -90,7 +90,7 @@ int pp_load_params(PPParameters *params, const char *filename,
 	char *errmsg, size_t errlen);
 
 /* Validate parameters against this implementation's limits (grid sides
- * 1..65535, grid_xy < 2^28, 1 <= grass_restart <= 65535, probabilities
+ * 1..65535, grid_xy < 2^30, 1 <= grass_restart <= 32767, probabilities
  * <= 100). Returns PP_SUCCESS or PP_INVALID_ARGS. */
 int pp_params_check(const PPParameters *params, char *errmsg, size_t errlen);
 

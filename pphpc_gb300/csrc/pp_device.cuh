@@ -3,6 +3,13 @@
  * Philox4x32-10, uniform integer draws, acquire/release accessors, the run
  * table and the per-world counters.
  *
+ * Grass layout: one uint16 per cell holding the run-local iteration at
+ * which the cell's grass is (or was) alive again, modulo 2^16; the
+ * countdown of iteration t is max(0, (int16)(regrow - t)). Cells are only
+ * read where agents are, and written when a sheep eats; the per-iteration
+ * grass stats come from a per-run histogram of pending regrowth
+ * iterations, updated by the eating events.
+ *
  * Agent layout (structure of arrays, one slot per agent):
  *   key[i] = global cell index (y * grid_x + x + run cell base), or the
  *            world's dead sentinel (= number of padded cells) after a move
@@ -127,6 +134,7 @@ struct RunDev {
 	uint32_t iters;            /* iterations this run performs             */
 	uint32_t start_giter;      /* world iteration at which iter 1 runs - 1 */
 	uint32_t active;           /* 0 = finished or empty slot               */
+	uint32_t fbase;            /* this run's regrowth histogram (restart+1 slots) */
 	fastdiv gxdiv;
 };
 

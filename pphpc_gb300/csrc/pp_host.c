@@ -119,8 +119,8 @@ int pp_params_check(const PPParameters *p, char *errmsg, size_t errlen)
 		set_msg(errmsg, errlen, "grid must have fewer than 2^30 cells");
 		return PP_INVALID_ARGS;
 	}
-	if (p->grass_restart < 1 || p->grass_restart > 65535) {
-		set_msg(errmsg, errlen, "GRASS_RESTART must be in 1..65535");
+	if (p->grass_restart < 1 || p->grass_restart > 32767) {
+		set_msg(errmsg, errlen, "GRASS_RESTART must be in 1..32767");
 		return PP_INVALID_ARGS;
 	}
 	if (p->sheep_reproduce_prob > 100 || p->wolves_reproduce_prob > 100) {

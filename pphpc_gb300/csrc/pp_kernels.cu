@@ -382,50 +382,20 @@ __device__ __forceinline__ void stats_atomic_add(PPStatistics *dst,
 	}
 }
 
-template <int CPT>
-__device__ __forceinline__ void load_grass(const uint16_t *gp, uint16_t *gr)
-{
-	if (CPT == 4) {
-		uint2 q = *reinterpret_cast<const uint2 *>(gp);
-		memcpy(gr, &q, 8);
-	} else {
-#pragma unroll
-		for (int q = 0; q < CPT; q += 8) {
-			uint4 v = *reinterpret_cast<const uint4 *>(gp + q);
-			memcpy(gr + q, &v, 16);
-		}
-	}
-}
-
-template <int CPT>
-__device__ __forceinline__ void store_grass(uint16_t *gp, const uint16_t *gr)
-{
-	if (CPT == 4) {
-		uint2 q;
-		memcpy(&q, gr, 8);
-		*reinterpret_cast<uint2 *>(gp) = q;
-	} else {
-#pragma unroll
-		for (int q = 0; q < CPT; q += 8) {
-			uint4 v;
-			memcpy(&v, gr + q, 16);
-			*reinterpret_cast<uint4 *>(gp + q) = v;
-		}
-	}
-}
-
 /* One CTA per tile of CPT * 256 cells, taken by ticket. Phases:
  *   (grouping)    the tile's agents arrive grouped by tile in canonical
- *                 order; a counting sort by cell in shared memory, each
- *                 cell's short list put back in arrival order;
- *   A (per cell)  grass countdown into shared memory, cells transposed
- *                 across threads so the 16-bit accesses do not conflict;
+ *                 order; a counting sort by cell in shared memory
+ *                 (counters transposed across threads so no two threads of
+ *                 a warp share a bank), each cell's short list put back in
+ *                 arrival order;
  *   B (per agent) priority and dice of every agent (its rank = distance
  *                 to its cell's first entry);
- *   C (per cell with agents, from its first agent) the cell's actions;
- *   D (per cell)  grass stats and vector store;
+ *   C (per occupied cell, from its first agent) the cell's grass
+ *                 countdown (from its regrowth iteration) and actions;
  *   E (per agent chunk) survivors and newborns, in list order, into the
- *                 tile's region [2 * a0, 2 * a0 + total), agent stats. */
+ *                 tile's region [2 * a0, 2 * a0 + total), agent stats.
+ * Cells without agents are not touched: the countdown decrement of
+ * pp_gpu.cl:448-476 is implicit in the regrowth representation. */
 template <int CPT>
 __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	const uint32_t *__restrict__ kS, uint32_t *__restrict__ vS)
@@ -434,7 +404,6 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	uint32_t *sk = sm, *sv = sm + w.act_cap, *sp = sv + w.act_cap,
 		*sd = sp + w.act_cap, *sperm = sd + w.act_cap;
 	uint32_t *scnt = sperm + w.act_cap;                 /* CPT * 256 */
-	uint16_t *sg = reinterpret_cast<uint16_t *>(scnt + CPT * ACT_THREADS);
 	__shared__ uint32_t s_tile;
 	__shared__ uint64_t s_part[6];
 	const uint32_t tid = threadIdx.x;
@@ -488,16 +457,6 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 #define SLOT(c) ((((c) % CPT) * ACT_THREADS) + (c) / CPT)
 #pragma unroll
 	for (int q = 0; q < CPT; q++) scnt[q * ACT_THREADS + tid] = 0;
-	/* A: countdown (cells past the run's grid are padding, untouched) */
-	uint16_t gr[CPT];
-	uint16_t *gp = w.grass + c0 + cell0;
-	load_grass<CPT>(gp, gr);
-#pragma unroll
-	for (int q = 0; q < CPT; q++) {
-		uint32_t gq = gr[q];
-		if (gq > 0 && (lt0 + cell0 + q) < ncells) gq--;
-		sg[q * ACT_THREADS + tid] = (uint16_t) gq;
-	}
 	__syncthreads();
 	/* counting sort of the tile's agents by cell */
 	for (uint32_t j = tid; j < m; j += ACT_THREADS) {
@@ -558,30 +517,27 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 		LD[j] = draw(r.y, 100);
 	}
 	__syncthreads();
-	/* C: actions, one thread per occupied cell (its first agent's) */
+	/* C: actions, one thread per occupied cell (its first agent's). The
+	 * cell's countdown is max(0, regrowth - t); a sheep that eats sets the
+	 * regrowth to t + restart, counted for the run's regrowth histogram. */
+	uint32_t eats = 0;
+	const uint16_t t16 = (uint16_t) t;
 	for (uint32_t j = tid; j < m; j += ACT_THREADS) {
 		const uint32_t lc = LK[j];
 		if (j > 0 && LK[j - 1] == lc) continue;
 		uint32_t e = j + 1;
 		while (e < m && LK[e] == lc) e++;
-		uint16_t *gs = &sg[(lc % CPT) * ACT_THREADS + lc / CPT];
-		uint32_t gq = *gs;
+		uint16_t *gptr = w.grass + c0 + lc;
+		const int32_t dd = (int16_t) (uint16_t) (*gptr - t16);
+		uint32_t gq = dd > 0 ? (uint32_t) dd : 0u;
+		const uint32_t g0 = gq;
 		act_cell(j, e, LV, LP, LD, ap, gq);
-		*gs = (uint16_t) gq;
+		if (gq != g0) {
+			*gptr = (uint16_t) (t16 + (uint16_t) ap.restart);
+			eats++;
+		}
 	}
 	__syncthreads();
-	/* D: grass stats and store */
-	uint32_t galive = 0, gsum = 0;
-#pragma unroll
-	for (int q = 0; q < CPT; q++) {
-		const uint32_t gq = sg[q * ACT_THREADS + tid];
-		if ((lt0 + cell0 + q) < ncells) {
-			galive += gq == 0;
-			gsum += gq;
-		}
-		gr[q] = (uint16_t) gq;
-	}
-	store_grass<CPT>(gp, gr);
 	/* E: outputs in list order, contiguous agent chunks per thread */
 	const uint32_t ch = (m + ACT_THREADS - 1) / ACT_THREADS;
 	const uint32_t ja = min(tid * ch, m), jb = min(ja + ch, m);
@@ -616,12 +572,16 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 			else { sheep++; sen += kd; }
 		}
 	}
-	/* per-tile partial stats */
+	/* per-tile partial stats; the tile's eating events go to the run's
+	 * regrowth histogram slot of iteration t + restart */
 	StatAcc acc;
-	acc.sheep = sheep; acc.wolves = wolves; acc.galive = galive;
-	acc.sen = sen; acc.wen = wen; acc.gen = gsum;
+	acc.sheep = sheep; acc.wolves = wolves; acc.galive = eats;
+	acc.sen = sen; acc.wen = wen; acc.gen = 0;
 	block_stats(acc, s_part);
-	if (tid < 6) w.part[(size_t) tile * 8 + tid] = s_part[tid];
+	if (tid < 6) w.part[(size_t) tile * 8 + tid] = (tid == 2 || tid == 5) ? 0 : s_part[tid];
+	if (tid == 0 && s_part[2])
+		atomicAdd(&w.fring[run.fbase + (t + ap.restart) % (ap.restart + 1)],
+			(uint32_t) s_part[2]);
 }
 
 /* Per chunk of tiles (chunks taken by ticket, so a chunk's predecessors are
@@ -673,6 +633,31 @@ __global__ void __launch_bounds__(256) k_finish(WorldDev w)
 				for (int f = 0; f < 6; f++)
 					stats_atomic_add(dst, f, w.part[(size_t) tl * 8 + f]);
 			}
+		}
+	}
+	if (FULL) {
+		/* grass stats of iteration t of every live run from its regrowth
+		 * histogram: pending regrowths r in (t, t + restart] are the dead
+		 * cells, each with countdown r - t. Slot t (cells alive again since
+		 * t) is cleared for the eating events of iteration t + 1, which
+		 * land at t + 1 + restart = t (mod restart + 1). */
+		for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < w.nruns_cap;
+			r += gridDim.x * blockDim.x) {
+			const RunDev &run = w.runs[r];
+			const uint32_t t = g - run.start_giter;
+			if (!run_live(run, t)) continue;
+			const uint32_t fs = run.restart + 1;
+			uint32_t *f = w.fring + run.fbase;
+			uint64_t dead = 0, sum = 0;
+			for (uint32_t k = 1; k <= run.restart; k++) {
+				const uint32_t c = f[(t + k) % fs];
+				dead += c;
+				sum += (uint64_t) k * c;
+			}
+			PPStatistics *dst = &w.ring[(size_t) row * w.nruns_cap + r];
+			stats_atomic_add(dst, 2, run.ncells - dead);
+			stats_atomic_add(dst, 5, sum);
+			f[t % fs] = 0;
 		}
 	}
 	/* dense bases of the regions */
@@ -755,8 +740,16 @@ __global__ void k_after_sort(WorldCounters *ctr, uint32_t *hist)
 /* Init and stats of a freshly initialised run                         */
 /* ------------------------------------------------------------------ */
 
+/* Initial grass of a run: countdown c (0 = alive) stored as the regrowth
+ * iteration c, and c counted in the run's regrowth histogram. */
 __global__ void k_init_grass(WorldDev w, RunDev run)
 {
+	__shared__ uint32_t sh[1024];
+	const uint32_t fs = run.restart + 1;
+	const bool local = fs <= 1024;
+	if (local)
+		for (uint32_t q = threadIdx.x; q < fs; q += blockDim.x) sh[q] = 0;
+	__syncthreads();
 	const uint32_t span = run.n_tiles << w.log_tile;
 	for (uint32_t lc = blockIdx.x * blockDim.x + threadIdx.x; lc < span;
 		lc += gridDim.x * blockDim.x) {
@@ -765,8 +758,34 @@ __global__ void k_init_grass(WorldDev w, RunDev run)
 			u4 r = rng(run.seed_lo, run.seed_hi, lc, 0, STREAM_INIT_CELL, 0);
 			uint32_t alive = draw(r.x, 2);
 			v = alive ? 0 : (uint16_t) (1 + draw(r.y, run.restart));
+			if (v) {
+				if (local) atomicAdd(&sh[v], 1u);
+				else atomicAdd(&w.fring[run.fbase + v], 1u);
+			}
 		}
 		w.grass[run.cbase + lc] = v;
+	}
+	__syncthreads();
+	if (local)
+		for (uint32_t q = threadIdx.x; q < fs; q += blockDim.x)
+			if (sh[q]) atomicAdd(&w.fring[run.fbase + q], sh[q]);
+}
+
+/* Every alive cell's regrowth iteration moved to the run's current
+ * iteration t (countdown 0 either way), so (int16)(regrowth - t) never
+ * wraps: run every few thousand iterations. */
+__global__ void k_grass_rebase(WorldDev w)
+{
+	const uint32_t gdone = w.ctr->giter;
+	const uint32_t cells = w.n_tiles << w.log_tile;
+	for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < cells;
+		c += gridDim.x * blockDim.x) {
+		const RunDev &run = w.runs[w.tile_run[c >> w.log_tile]];
+		const uint32_t t = gdone - run.start_giter;
+		if (!run.active || c - run.cbase >= run.ncells) continue;
+		const uint16_t t16 = (uint16_t) t;
+		const int32_t dd = (int16_t) (uint16_t) (w.grass[c] - t16);
+		if (dd < 0) w.grass[c] = t16;
 	}
 }
 
@@ -849,9 +868,9 @@ cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
 		w.log_tile, w.n_tiles, w.tile_off);
 	if (marks) cudaEventRecord(marks[2 + w.passes], s);
 	size_t act_smem = (size_t) w.act_cap * 5 * sizeof(uint32_t)
-		+ ((size_t) lc.cpt * ACT_THREADS) * (sizeof(uint32_t) + sizeof(uint16_t));
-	/* (the shared-memory layout of k_act: five agent arrays, then per-cell
-	 * counters and countdowns of the tile) */
+		+ ((size_t) lc.cpt * ACT_THREADS) * sizeof(uint32_t);
+	/* (the shared-memory layout of k_act: five agent arrays, then the
+	 * tile's per-cell counters) */
 	switch (lc.cpt) {
 	case 4: k_act<4><<<w.n_tiles, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
 	case 16: k_act<16><<<w.n_tiles, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
@@ -929,6 +948,13 @@ cudaError_t enqueue_compact(const WorldDev &w, const LaunchCfg &lc,
 	uint32_t *ko, uint32_t *vo, cudaStream_t s)
 {
 	k_regions<false><<<lc.move_blocks, 256, 0, s>>>(w, ko, vo);
+	return cudaGetLastError();
+}
+
+cudaError_t enqueue_grass_rebase(const WorldDev &w, const LaunchCfg &lc,
+	cudaStream_t s)
+{
+	k_grass_rebase<<<lc.sms * 8, 256, 0, s>>>(w);
 	return cudaGetLastError();
 }
 

@@ -16,7 +16,8 @@ namespace pp {
  * B <-> C, the act reads the sorted array and writes each tile's region
  * at twice its sorted offset. A (cap slots) is a dense copy for read-back. */
 struct WorldDev {
-	uint16_t *grass;          /* n_tiles << log_tile cells                 */
+	uint16_t *grass;          /* regrowth iteration per cell (see pp_device.cuh) */
+	uint32_t *fring;          /* per-run histograms of pending regrowth iterations */
 	uint32_t *kA, *vA, *kB, *vB, *kC, *vC;
 	uint32_t *kR, *vR;        /* region buffer, 3 * cap slots              */
 	uint32_t *rstart, *rcnt;  /* n_tiles                                   */
@@ -74,6 +75,10 @@ cudaError_t enqueue_regions_from_sorted(const WorldDev &w, const LaunchCfg &lc,
 /* Dense copy of all regions into ko/vo (dbase order). */
 cudaError_t enqueue_compact(const WorldDev &w, const LaunchCfg &lc,
 	uint32_t *ko, uint32_t *vo, cudaStream_t s);
+/* Move the regrowth iteration of alive cells to their run's current
+ * iteration (keeps the 16-bit representation from wrapping). */
+cudaError_t enqueue_grass_rebase(const WorldDev &w, const LaunchCfg &lc,
+	cudaStream_t s);
 /* After a standalone sort that used the world's counters: new look-back
  * epochs, fresh tickets, zero histograms. */
 cudaError_t enqueue_after_sort(WorldCounters *ctr, uint32_t *hist,

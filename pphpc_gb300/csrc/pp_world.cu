@@ -82,7 +82,7 @@ int World::alloc(size_t bytes, void **p)
 }
 
 static RunDev make_run(const RunSpec &s, uint32_t first_tile,
-	uint32_t n_tiles, uint32_t log_tile, uint32_t start_giter)
+	uint32_t n_tiles, uint32_t log_tile, uint32_t start_giter, uint32_t fbase)
 {
 	RunDev r{};
 	r.gx = s.p.grid_x;
@@ -103,6 +103,7 @@ static RunDev make_run(const RunSpec &s, uint32_t first_tile,
 	r.iters = s.iters;
 	r.start_giter = start_giter;
 	r.active = 1;
+	r.fbase = fbase;
 	r.gxdiv = fastdiv_make(s.p.grid_x);
 	return r;
 }
@@ -205,6 +206,17 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	PP_AL(w_.ctr, sizeof(WorldCounters));
 	PP_AL(w_.hist, 8 * 256 * 4);
 	PP_AL(w_.ring, (size_t) w_.ring_rows * nruns_cap * sizeof(PPStatistics));
+	/* regrowth histograms: restart + 1 slots per initial run, and room for
+	 * any restart in every slot left for later admissions */
+	std::vector<uint32_t> fbase_h(runs.size());
+	uint64_t fsz = 0;
+	for (size_t r = 0; r < runs.size(); r++) {
+		fbase_h[r] = (uint32_t) fsz;
+		fsz += runs[r].p.grass_restart + 1;
+	}
+	fslot_base_ = (uint32_t) fsz;
+	fsz += (uint64_t) (nruns_cap - 1 - runs.size()) * FSLOT;
+	PP_AL(w_.fring, std::max<uint64_t>(fsz, 1) * 4);
 #undef PP_AL
 	PP_CK(cudaMemsetAsync(w_.lb_sort, 0, sort_tiles * 256 * sizeof(uint64_t), s_));
 	PP_CK(cudaMemsetAsync(w_.lb_fin, 0, ((size_t) tiles + 1) * sizeof(uint64_t), s_));
@@ -213,6 +225,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	PP_CK(cudaMemsetAsync(w_.hist, 0, 8 * 256 * 4, s_));
 	PP_CK(cudaMemsetAsync(w_.ring, 0, (size_t) w_.ring_rows * nruns_cap * sizeof(PPStatistics), s_));
 	PP_CK(cudaMemsetAsync(w_.part, 0, (size_t) tiles * 8 * sizeof(uint64_t), s_));
+	PP_CK(cudaMemsetAsync(w_.fring, 0, std::max<uint64_t>(fsz, 1) * 4, s_));
 
 	/* Run table and tile map. */
 	runs_h_.assign(nruns_cap, RunDev{});
@@ -221,7 +234,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	std::vector<uint32_t> base_h(nruns_cap, 0);
 	uint32_t base = 0;
 	for (size_t r = 0; r < runs.size(); r++) {
-		runs_h_[r] = make_run(runs[r], first[r], ntl[r], log_tile, 0);
+		runs_h_[r] = make_run(runs[r], first[r], ntl[r], log_tile, 0, fbase_h[r]);
 		for (uint32_t t = 0; t < ntl[r]; t++) tile_run_h_[first[r] + t] = (uint16_t) r;
 		base_h[r] = base;
 		base += runs[r].p.init_sheep + runs[r].p.init_wolves;
@@ -325,15 +338,24 @@ int World::build_graph()
 int World::enqueue(uint32_t n)
 {
 	PP_CK(cudaSetDevice(device_));
+	/* iterations run in stretches that end on multiples of REBASE, where
+	 * the grass regrowth iterations are re-based (16-bit wrap-around) */
 	uint32_t done = 0;
-	if (gexec_ && graph_iters_) {
-		while (n - done >= graph_iters_) {
-			PP_CK(cudaGraphLaunch(gexec_, s_));
-			done += graph_iters_;
+	while (done < n) {
+		uint32_t to_rebase = REBASE - (giter_ % REBASE);
+		uint32_t stretch = std::min(n - done, to_rebase);
+		uint32_t k = 0;
+		if (gexec_ && graph_iters_) {
+			while (stretch - k >= graph_iters_) {
+				PP_CK(cudaGraphLaunch(gexec_, s_));
+				k += graph_iters_;
+			}
 		}
+		for (; k < stretch; k++) PP_CK(enqueue_iteration(w_, lc_, s_));
+		giter_ += stretch;
+		done += stretch;
+		if (giter_ % REBASE == 0) PP_CK(enqueue_grass_rebase(w_, lc_, s_));
 	}
-	for (; done < n; done++) PP_CK(enqueue_iteration(w_, lc_, s_));
-	giter_ += n;
 	if (n) {
 		release_pending();
 		adm_used_ = 0;   /* the act rewrote every region below 2 * cap */
@@ -396,9 +418,15 @@ int World::get_state(uint32_t *cell, uint32_t *en, uint32_t n_max,
 	if (cell && m) PP_CK(cudaMemcpy(cell, w_.kA, (size_t) m * 4, cudaMemcpyDeviceToHost));
 	if (en && m) PP_CK(cudaMemcpy(en, w_.vA, (size_t) m * 4, cudaMemcpyDeviceToHost));
 	if (grass) {
+		/* stored regrowth iterations -> countdowns of the current iteration */
 		const RunDev &run = runs_h_[r];
 		PP_CK(cudaMemcpy(grass, w_.grass + run.cbase,
 			(size_t) run.ncells * 2, cudaMemcpyDeviceToHost));
+		const uint16_t t16 = (uint16_t) (giter_ - run.start_giter);
+		for (uint32_t c = 0; c < run.ncells; c++) {
+			const int32_t dd = (int16_t) (uint16_t) (grass[c] - t16);
+			grass[c] = (uint16_t) (dd > 0 ? dd : 0);
+		}
 	}
 	if (cell && m) {
 		/* Report cells relative to the run's grid. */
@@ -448,7 +476,9 @@ int World::profile(uint32_t n, pp_kernel_prof *prof, double *agent_steps)
 		prof[2].bytes += 4.0 * n_before + 4.0 * (w_.n_tiles + 1);
 		PP_CK(cudaEventElapsedTime(&ms, ev[2 + P], ev[3 + P]));
 		prof[3].launches++; prof[3].total_ms += ms;
-		prof[3].bytes += 4.0 * live_cells + 8.0 * n_live + 8.0 * n_after;
+		/* act: sorted agents in, survivors and newborns out, the regrowth
+		 * word of each occupied cell (at most one per agent) */
+		prof[3].bytes += 10.0 * n_live + 8.0 * n_after;
 		PP_CK(cudaEventElapsedTime(&ms, ev[3 + P], ev[4 + P]));
 		prof[4].launches++; prof[4].total_ms += ms;
 		prof[4].bytes += 48.0 * w_.n_tiles;
@@ -497,7 +527,9 @@ int World::admit(const RunSpec &spec, uint32_t *slot_out)
 		free_tiles_.push_back({first, need});
 		return PP_OUT_OF_RESOURCES;
 	}
-	RunDev run = make_run(spec, first, need, w_.log_tile, giter_);
+	const uint32_t fbase = fslot_base_ + slot * FSLOT;
+	RunDev run = make_run(spec, first, need, w_.log_tile, giter_, fbase);
+	PP_CK(cudaMemsetAsync(w_.fring + fbase, 0, (spec.p.grass_restart + 1) * 4, s_));
 	runs_h_[slot] = run;
 	for (uint32_t t = 0; t < need; t++) tile_run_h_[first + t] = (uint16_t) slot;
 	PP_CK(cudaMemcpyAsync(&w_.runs[slot], &run, sizeof(RunDev), cudaMemcpyHostToDevice, s_));
@@ -809,7 +841,7 @@ extern "C" int pp_move_host(const PPParameters *params, uint64_t seed,
 	s.p = *params;
 	s.seed = seed;
 	s.iters = 0xffffffffu;
-	RunDev run = make_run(s, 0, 1, 0, 0);
+	RunDev run = make_run(s, 0, 1, 0, 0, 0);
 	DevBuf ki, vi, ko, vo, rd;
 	size_t b = (size_t) n * 4;
 	PP_CK(ki.alloc(b)); PP_CK(vi.alloc(b)); PP_CK(ko.alloc(b)); PP_CK(vo.alloc(b));

@@ -102,6 +102,9 @@ private:
 	void release_pending();
 	uint32_t agents_reserved_ = 0;
 	uint32_t adm_used_ = 0;   /* admission area of the region buffer in use */
+	uint32_t fslot_base_ = 0; /* regrowth histograms of admitted runs start here */
+	static constexpr uint32_t FSLOT = 32768;   /* histogram room per admitted run */
+	static constexpr uint32_t REBASE = 8192;   /* iterations between re-basings */
 public:
 	uint64_t h2d_ = 0, d2h_ = 0;   /* bytes copied host<->device by the world */
 private:
