@@ -147,7 +147,7 @@ struct WorldCounters {
 	uint32_t giter;          /* world iterations completed               */
 	uint32_t seq;            /* look-back epoch base, +1 per iteration   */
 	uint32_t err;            /* ERRF_* bits                              */
-	uint32_t act_ticket;     /* act tile tickets                          */
+	uint32_t act_ticket;     /* unused (kept for layout)                   */
 	uint32_t finish_done;    /* finish CTAs done                          */
 	uint32_t sort_ticket[8]; /* one per radix pass                        */
 	uint32_t aux_n;          /* element count of a standalone sort        */

@@ -215,6 +215,27 @@ __device__ __forceinline__ void act_cell(uint32_t p, uint32_t e,
 	uint32_t *LV, const uint32_t *LP, uint32_t *LD, const ActParams &ap,
 	uint32_t &g)
 {
+	if (e - p == 1) {
+		/* alone in its cell: a sheep acts and is not eaten, a wolf finds
+		 * no sheep */
+		const uint32_t v = LV[p], tb = v & TYPE_BIT;
+		uint32_t en = v & ENERGY_MASK, thr, prob;
+		if (tb) {
+			thr = ap.wolves_thr;
+			prob = ap.wolves_prob;
+		} else {
+			if (g == 0) {
+				g = ap.restart;
+				en += ap.sheep_gain;
+			}
+			thr = ap.sheep_thr;
+			prob = ap.sheep_prob;
+		}
+		const uint32_t kid = (en > thr && LD[p] < prob) ? en >> 1 : 0;
+		LV[p] = tb | (en - kid);
+		LD[p] = kid;
+		return;
+	}
 	uint32_t S = 0, W = 0;
 	for (uint32_t j = p; j < e; j++) {
 		if (LV[j] & TYPE_BIT) W++;
@@ -382,7 +403,8 @@ __device__ __forceinline__ void stats_atomic_add(PPStatistics *dst,
 	}
 }
 
-/* One CTA per tile of CPT * 256 cells, taken by ticket. Phases:
+/* One CTA per tile of CPT * 256 cells (tiles do not depend on each other).
+ * Phases:
  *   (grouping)    the tile's agents arrive grouped by tile in canonical
  *                 order; a counting sort by cell in shared memory
  *                 (counters transposed across threads so no two threads of
@@ -397,20 +419,15 @@ __device__ __forceinline__ void stats_atomic_add(PPStatistics *dst,
  * Cells without agents are not touched: the countdown decrement of
  * pp_gpu.cl:448-476 is implicit in the regrowth representation. */
 template <int CPT>
-__global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
+__global__ void __launch_bounds__(ACT_THREADS, 5) k_act(WorldDev w,
 	const uint32_t *__restrict__ kS, uint32_t *__restrict__ vS)
 {
 	extern __shared__ uint32_t sm[];
 	uint32_t *sk = sm, *sv = sm + w.act_cap, *sp = sv + w.act_cap,
 		*sd = sp + w.act_cap, *sperm = sd + w.act_cap;
 	uint32_t *scnt = sperm + w.act_cap;                 /* CPT * 256 */
-	__shared__ uint32_t s_tile;
-	__shared__ uint64_t s_part[6];
 	const uint32_t tid = threadIdx.x;
-	if (tid == 0) s_tile = atomicAdd(&w.ctr->act_ticket, 1u);
-	__syncthreads();
-	const uint32_t tile = s_tile;
-	if (tile >= w.n_tiles) return;
+	const uint32_t tile = blockIdx.x;   /* tiles are independent */
 	const uint32_t g = w.ctr->giter + 1;
 	const RunDev &run = w.runs[w.tile_run[tile]];
 	const uint32_t t = g - run.start_giter;
@@ -459,6 +476,7 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	for (int q = 0; q < CPT; q++) scnt[q * ACT_THREADS + tid] = 0;
 	__syncthreads();
 	/* counting sort of the tile's agents by cell */
+	uint32_t multi = 0;   /* this thread's cells holding two or more agents */
 	for (uint32_t j = tid; j < m; j += ACT_THREADS) {
 		const uint32_t lc = UK[j] - c0;
 		atomicAdd(&scnt[SLOT(lc)], 1u);
@@ -467,7 +485,11 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	{
 		uint32_t loc = 0;
 #pragma unroll
-		for (int q = 0; q < CPT; q++) loc += scnt[q * ACT_THREADS + tid];
+		for (int q = 0; q < CPT; q++) {
+			const uint32_t c = scnt[q * ACT_THREADS + tid];
+			loc += c;
+			if (c > 1) multi |= 1u << q;
+		}
 		uint32_t tot;
 		uint32_t run_start = block_excl_scan(loc, &tot);
 #pragma unroll
@@ -484,19 +506,17 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	}
 	__syncthreads();
 	/* scnt[SLOT(c)] is now the end of cell c; restore the arrival order of
-	 * each cell's (short) list */
-	{
-		uint32_t b = tid ? scnt[(CPT - 1) * ACT_THREADS + tid - 1] : 0;
-#pragma unroll 1
-		for (int q = 0; q < CPT; q++) {
-			const uint32_t e = scnt[q * ACT_THREADS + tid];
-			for (uint32_t i = b + 1; i < e; i++) {
-				const uint32_t x = PERM[i];
-				uint32_t h = i;
-				while (h > b && PERM[h - 1] > x) { PERM[h] = PERM[h - 1]; h--; }
-				PERM[h] = x;
-			}
-			b = e;
+	 * each cell's list (only cells holding two or more agents) */
+	while (multi) {
+		const int q = __ffs(multi) - 1;
+		multi &= multi - 1;
+		const uint32_t c = cell0 + q;
+		const uint32_t b = c ? scnt[SLOT(c - 1)] : 0, e = scnt[SLOT(c)];
+		for (uint32_t i = b + 1; i < e; i++) {
+			const uint32_t x = PERM[i];
+			uint32_t h = i;
+			while (h > b && PERM[h - 1] > x) { PERM[h] = PERM[h - 1]; h--; }
+			PERM[h] = x;
 		}
 	}
 #undef SLOT
@@ -574,14 +594,34 @@ __global__ void __launch_bounds__(ACT_THREADS) k_act(WorldDev w,
 	}
 	/* per-tile partial stats; the tile's eating events go to the run's
 	 * regrowth histogram slot of iteration t + restart */
-	StatAcc acc;
-	acc.sheep = sheep; acc.wolves = wolves; acc.galive = eats;
-	acc.sen = sen; acc.wen = wen; acc.gen = 0;
-	block_stats(acc, s_part);
-	if (tid < 6) w.part[(size_t) tile * 8 + tid] = (tid == 2 || tid == 5) ? 0 : s_part[tid];
-	if (tid == 0 && s_part[2])
-		atomicAdd(&w.fring[run.fbase + (t + ap.restart) % (ap.restart + 1)],
-			(uint32_t) s_part[2]);
+	{
+		__shared__ uint64_t red[5][ACT_THREADS / 32];
+		const uint32_t lane = tid & 31, wid = tid >> 5;
+		const uint32_t sw = warp_sum(sheep | (wolves << 16));
+		const uint32_t ew = warp_sum(eats);
+		const uint64_t se = warp_sum(sen), we = warp_sum(wen);
+		if (lane == 0) {
+			red[0][wid] = sw & 0xffffu;
+			red[1][wid] = sw >> 16;
+			red[2][wid] = ew;
+			red[3][wid] = se;
+			red[4][wid] = we;
+		}
+		__syncthreads();
+		if (tid < 5) {
+			uint64_t sum = 0;
+			for (uint32_t q = 0; q < ACT_THREADS / 32; q++) sum += red[tid][q];
+			if (tid == 2) {
+				if (sum)
+					atomicAdd(&w.fring[run.fbase + (t + ap.restart) % (ap.restart + 1)],
+						(uint32_t) sum);
+				w.part[(size_t) tile * 8 + 2] = 0;
+				w.part[(size_t) tile * 8 + 5] = 0;
+			} else {
+				w.part[(size_t) tile * 8 + tid] = sum;
+			}
+		}
+	}
 }
 
 /* Per chunk of tiles (chunks taken by ticket, so a chunk's predecessors are
