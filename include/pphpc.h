@@ -118,8 +118,10 @@ typedef struct pp_opts {
 	uint32_t tile_cells;    /* cells per act tile (power of 2); 0 = autotune  */
 	uint32_t sort_digit_bits; /* radix digit width 4..8; 0 = autotune         */
 	uint32_t use_graph;     /* capture each iteration as a CUDA graph (1) or not (0) */
-	uint32_t unfused;       /* 1 = reference-shaped pipeline: dense per-cell
-	                           offsets + separate grass kernel; 0 = fused tiles */
+	uint32_t sort_pipeline; /* 1 = per-iteration sort pipeline (move, LSD radix
+	                           passes over the tile bits, tile offsets, act);
+	                           0 = fused act+move with a gather by destination
+	                           tile (default) */
 } pp_opts;
 
 /* Fill `opts` with defaults. */

@@ -74,7 +74,7 @@ class PPStatistics(C.Structure):
 class PPOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("max_agents", C.c_uint32),
                 ("tile_cells", C.c_uint32), ("sort_digit_bits", C.c_uint32),
-                ("use_graph", C.c_uint32), ("unfused", C.c_uint32)]
+                ("use_graph", C.c_uint32), ("sort_pipeline", C.c_uint32)]
 
 
 class PPRunDesc(C.Structure):
@@ -212,7 +212,7 @@ class Simulation:
     """One PPHPC run on the GPU (pp_sim_* of the C ABI)."""
 
     def __init__(self, params, seed=0, device=0, max_agents=0, tile_cells=0,
-                 digit_bits=0, use_graph=True):
+                 digit_bits=0, use_graph=True, sort_pipeline=False):
         L = lib()
         o = PPOpts()
         L.pp_opts_default(C.byref(o))
@@ -221,6 +221,7 @@ class Simulation:
         o.tile_cells = tile_cells
         o.sort_digit_bits = digit_bits
         o.use_graph = 1 if use_graph else 0
+        o.sort_pipeline = 1 if sort_pipeline else 0
         self.params = params
         self._h = C.c_void_p()
         _check(L.pp_sim_create(C.byref(params), seed, C.byref(o), C.byref(self._h)),
@@ -273,7 +274,10 @@ class Simulation:
 
     def state(self):
         import numpy as np
-        _, n, _ = self.info()
+        cnt = C.c_uint32()
+        _check(lib().pp_sim_get_state(self._h, None, None, 0, C.byref(cnt), None),
+               "pp_sim_get_state")
+        n = cnt.value
         cell = np.zeros(max(n, 1), np.uint32)
         en = np.zeros(max(n, 1), np.uint32)
         grass = np.zeros(self.params.grid_x * self.params.grid_y, np.uint16)

@@ -1,0 +1,208 @@
+/*
+ * pp_act.cuh -- device logic shared by the sort pipeline (pp_kernels.cu)
+ * and the fused act+move pipeline (pp_fused.cu): the random walk and its
+ * inverse, the actions of one cell's agents, stats accumulation.
+ */
+#pragma once
+
+#include "pp_kernels.cuh"
+#include "pp_block.cuh"
+
+namespace pp {
+
+/* Run-local cell reached from run-local cell lc by direction dir of the
+ * 5-way random walk (0 stay, 1 +x, 2 -x, 3 +y, 4 -y; per-row and
+ * per-column wrap, pp_gpu.cl:756-819). */
+__device__ __forceinline__ uint32_t move_dir(const RunDev &run, uint32_t lc,
+	uint32_t dir)
+{
+	uint32_t y = fastdiv_div(lc, run.gxdiv);
+	uint32_t x = lc - y * run.gx;
+	if (dir == 1) x = (x + 1 == run.gx) ? 0 : x + 1;
+	else if (dir == 2) x = (x == 0) ? run.gx - 1 : x - 1;
+	else if (dir == 3) y = (y + 1 == run.gy) ? 0 : y + 1;
+	else if (dir == 4) y = (y == 0) ? run.gy - 1 : y - 1;
+	return y * run.gx + x;
+}
+
+/* Offset from destination cell (x, y) back to the cell an agent that moved
+ * in direction dir came from (the inverse of move_dir). */
+__host__ __device__ __forceinline__ int32_t src_offset(uint32_t dir,
+	uint32_t x, uint32_t y, uint32_t gx, uint32_t gy)
+{
+	switch (dir) {
+	case 1: return x == 0 ? (int32_t) (gx - 1) : -1;
+	case 2: return x == gx - 1 ? -(int32_t) (gx - 1) : 1;
+	case 3: return y == 0 ? (int32_t) ((gy - 1) * gx) : -(int32_t) gx;
+	case 4: return y == gy - 1 ? -(int32_t) ((gy - 1) * gx) : (int32_t) gx;
+	default: return 0;
+	}
+}
+
+/* Energy loss, death and toroidal random walk of one agent of rank k in
+ * its cell (pp_gpu.cl:756-819). */
+__device__ __forceinline__ void move_one(const RunDev &run, uint32_t key,
+	uint32_t val, uint32_t k, uint32_t t, uint32_t dead_key,
+	uint32_t &nk, uint32_t &nv)
+{
+	uint32_t e = val & ENERGY_MASK;
+	if (e <= 1) {
+		nk = dead_key;
+		nv = val & TYPE_BIT;
+		return;
+	}
+	uint32_t lc = key - run.cbase;
+	u4 r = rng(run.seed_lo, run.seed_hi, lc, t, STREAM_MOVE, k);
+	nk = run.cbase + move_dir(run, lc, draw(r.x, 5));
+	nv = val - 1;
+}
+
+__device__ __forceinline__ bool run_live(const RunDev &run, uint32_t t)
+{
+	return run.active && t >= 1 && t <= run.iters;
+}
+
+/* Model parameters the actions need, held in registers. */
+struct ActParams {
+	uint32_t sheep_gain, sheep_thr, sheep_prob;
+	uint32_t wolves_gain, wolves_thr, wolves_prob;
+	uint32_t restart;
+};
+
+/* Actions of the agents of one cell, entries [p, e) of the tile's agent
+ * list in cell-list order, in increasing (priority, rank) order; on entry
+ * LP[j] / LD[j] hold the priority and the dice of the agent of rank j - p,
+ * drawn from Philox({cell, t, ACT, rank}). This is the sequential semantics
+ * of pp_cpu.cl:640-848 (wolves eat the first not-yet-eaten sheep of the
+ * cell; a sheep acts only if not eaten before its turn; the first acting
+ * sheep takes live grass; every acting agent may reproduce) in closed form:
+ * the k-th wolf eats the k-th sheep, and a sheep acts iff the wolves before
+ * it are no more than the sheep before it.
+ * On return LV[j] holds type | final energy (energy 0 = eaten) and LD[j]
+ * the newborn's energy (0 = none). */
+__device__ __forceinline__ void act_cell(uint32_t p, uint32_t e,
+	uint32_t *LV, const uint32_t *LP, uint32_t *LD, const ActParams &ap,
+	uint32_t &g)
+{
+	if (e - p == 1) {
+		/* alone in its cell: a sheep acts and is not eaten, a wolf finds
+		 * no sheep */
+		const uint32_t v = LV[p], tb = v & TYPE_BIT;
+		uint32_t en = v & ENERGY_MASK, thr, prob;
+		if (tb) {
+			thr = ap.wolves_thr;
+			prob = ap.wolves_prob;
+		} else {
+			if (g == 0) {
+				g = ap.restart;
+				en += ap.sheep_gain;
+			}
+			thr = ap.sheep_thr;
+			prob = ap.sheep_prob;
+		}
+		const uint32_t kid = (en > thr && LD[p] < prob) ? en >> 1 : 0;
+		LV[p] = tb | (en - kid);
+		LD[p] = kid;
+		return;
+	}
+	uint32_t S = 0, W = 0;
+	for (uint32_t j = p; j < e; j++) {
+		if (LV[j] & TYPE_BIT) W++;
+		else S++;
+	}
+	uint32_t sb = 0, wb = 0;
+	uint32_t lp = 0;
+	uint32_t ls = 0xffffffffu; /* none selected yet */
+	const uint32_t m = e - p;
+	for (uint32_t step = 0; step < m; step++) {
+		uint32_t best = p;
+		if (m > 1) {
+			uint32_t bp = 0xffffffffu;
+			bool found = false;
+			for (uint32_t j = p; j < e; j++) {
+				uint32_t pj = LP[j];
+				bool after = (ls == 0xffffffffu) || pj > lp
+					|| (pj == lp && j > ls);
+				if (after && (!found || pj < bp)) {
+					best = j;
+					bp = pj;
+					found = true;
+				}
+			}
+		}
+		uint32_t v = LV[best];
+		uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
+		uint32_t dice = LD[best];
+		bool acts, eaten = false;
+		uint32_t thr, prob;
+		if (tb) {
+			if (wb < S) en += ap.wolves_gain;
+			wb++;
+			acts = true;
+			thr = ap.wolves_thr;
+			prob = ap.wolves_prob;
+		} else {
+			acts = wb <= sb;
+			eaten = sb < W;
+			sb++;
+			if (acts && g == 0) {
+				g = ap.restart;
+				en += ap.sheep_gain;
+			}
+			thr = ap.sheep_thr;
+			prob = ap.sheep_prob;
+		}
+		uint32_t kid = 0;
+		if (acts && en > thr && dice < prob) {
+			kid = en >> 1;
+			en -= kid;
+		}
+		LV[best] = tb | (eaten ? 0u : en);
+		LD[best] = kid;
+		lp = LP[best];
+		ls = best;
+	}
+}
+
+struct StatAcc {
+	uint32_t sheep, wolves, galive;
+	uint64_t sen, wen, gen;
+	__device__ void zero() { sheep = wolves = galive = 0; sen = wen = gen = 0; }
+};
+
+/* Block-reduce the per-thread stats into out[0..5] (u64, thread f writes
+ * field f). Must be called by all threads of the block. */
+__device__ __forceinline__ void block_stats(const StatAcc &a, uint64_t *out)
+{
+	__shared__ uint64_t red[6][ACT_THREADS / 32];
+	uint64_t v[6] = {a.sheep, a.wolves, a.galive, a.sen, a.wen, a.gen};
+	const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+	for (int f = 0; f < 6; f++) {
+		v[f] = warp_sum(v[f]);
+		if (lane == 0) red[f][wid] = v[f];
+	}
+	__syncthreads();
+	if (threadIdx.x < 6) {
+		uint64_t s = 0;
+		for (uint32_t q = 0; q < ACT_THREADS / 32; q++) s += red[threadIdx.x][q];
+		out[threadIdx.x] = s;
+	}
+	__syncthreads();
+}
+
+__device__ __forceinline__ void stats_atomic_add(PPStatistics *dst,
+	uint32_t f, uint64_t s)
+{
+	if (!s) return;
+	switch (f) {
+	case 0: atomicAdd(&dst->sheep, (uint32_t) s); break;
+	case 1: atomicAdd(&dst->wolves, (uint32_t) s); break;
+	case 2: atomicAdd(&dst->grass, (uint32_t) s); break;
+	case 3: atomicAdd((unsigned long long *) &dst->sheep_en, s); break;
+	case 4: atomicAdd((unsigned long long *) &dst->wolves_en, s); break;
+	default: atomicAdd((unsigned long long *) &dst->grass_en, s); break;
+	}
+}
+
+} /* namespace pp */

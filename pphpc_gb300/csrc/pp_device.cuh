@@ -42,6 +42,20 @@ enum : uint32_t {
 	ERRF_TIMEOUT = 2u,  /* a look-back wait hit its iteration limit      */
 };
 
+/* Fused pipeline records (group buffers): key = destination cell within
+ * its tile (bits 0-12) | move direction (bits 13-15; DIR_PARKED: not moved
+ * because the run ended, DIR_DEAD: died in the move) | rank of the agent in
+ * its source cell's list (bits 16-31); value = type | energy after the
+ * move (before it for parked and dead records). */
+constexpr uint32_t REC_DIR_SHIFT = 13;
+constexpr uint32_t REC_RANK_SHIFT = 16;
+constexpr uint32_t REC_RANK_MAX = 0xffffu;
+constexpr uint32_t DIR_PARKED = 6;
+constexpr uint32_t DIR_DEAD = 7;
+/* Inbox entries per tile and parity: {group start, count | GROUP_GRAVE}. */
+constexpr uint32_t IBX = 32;
+constexpr uint32_t GROUP_GRAVE = 0x80000000u;
+
 /* Philox4x32-10 (Salmon et al., SC'11), written from the paper. */
 struct u4 { uint32_t x, y, z, w; };
 
@@ -143,16 +157,17 @@ struct RunDev {
  * one, so a whole iteration is a fixed launch sequence (captured as a
  * graph). */
 struct WorldCounters {
-	uint32_t n_agents;       /* live agents in the pre-move array        */
+	uint32_t n_agents;       /* agents after the last act (stats count)  */
 	uint32_t giter;          /* world iterations completed               */
 	uint32_t seq;            /* look-back epoch base, +1 per iteration   */
 	uint32_t err;            /* ERRF_* bits                              */
-	uint32_t act_ticket;     /* unused (kept for layout)                   */
+	uint32_t xtop;           /* fused act: scratch slots taken by crowded tiles */
 	uint32_t finish_done;    /* finish CTAs done                          */
 	uint32_t sort_ticket[8]; /* one per radix pass                        */
 	uint32_t aux_n;          /* element count of a standalone sort        */
 	uint32_t fin_ticket;     /* finish chunk tickets                      */
-	uint32_t pad[2];
+	uint32_t n_all;          /* fused finish: records counted so far       */
+	uint32_t pad;
 };
 
 /* ---- memory-ordering helpers ---- */

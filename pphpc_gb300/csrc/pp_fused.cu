@@ -1,0 +1,663 @@
+/*
+ * pp_fused.cu -- the fused iteration: one kernel per iteration does the
+ * act of iteration t and the move of iteration t + 1 (opencl/pp/pp_gpu.cl
+ * action_agent 883-979 followed by move_agent 744-821), so no sort runs
+ * between the two.
+ *
+ * State between iterations (per parity of the world iteration):
+ *   group buffer  records of moved agents (pp_device.cuh), written by the
+ *                 act of each source tile as one contiguous group per
+ *                 destination tile it sends to (plus one group of dead and
+ *                 parked records), at twice the tile's dense input base;
+ *   inboxes       per destination tile, up to IBX {start, count} entries
+ *                 naming the groups destined to it.
+ * The act of a tile gathers its groups, groups its agents by cell (counting
+ * sort in shared memory), puts each cell's list in canonical order (source
+ * cell, rank in the source cell's list: both are in the record), runs the
+ * cells' actions exactly as the sort pipeline does, and then moves every
+ * survivor and newborn: the move draw is keyed by (cell, t + 1, MOVE, rank
+ * in the cell's new list), which the act knows. Positions inside a group
+ * are arbitrary, because the next act orders each cell's list by the
+ * record's (source cell, rank) and not by position. The finish kernel
+ * sums each tile's posted group sizes into the dense input bases of the
+ * next act, so no act allocates with an atomic on a shared counter.
+ */
+#include "pp_act.cuh"
+
+namespace pp {
+
+cudaError_t launch_finish_fused(const WorldDev &w, const LaunchCfg &lc,
+	cudaStream_t s);
+
+namespace {
+
+static_assert(IBX == 32, "the inbox is read by one warp");
+
+constexpr int NT = 128;                 /* threads per tile CTA (eight CTAs per SM) */
+constexpr uint32_t NCLS = 32;          /* group classes of a tile (one per lane) */
+constexpr uint32_t CLS_FOREIGN = 30;   /* classes 0..29: other destination tiles */
+constexpr uint32_t CLS_OWN = 30;       /* moved within the tile                  */
+constexpr uint32_t CLS_GRAVE = 31;     /* dead and parked records                */
+constexpr uint32_t CLS_NONE = 0xffffffffu;   /* table full: record dropped (error) */
+constexpr uint32_t TBL_EMPTY = 0xffffffffu;
+
+/* Class of destination tile dt (not the CTA's own tile) in the CTA's table
+ * of destination tiles, inserted when new; CLS_NONE if the table is full
+ * (a tile sends to at most 15 other tiles, so this does not happen). */
+__device__ __forceinline__ uint32_t class_insert(uint32_t *tbl, uint32_t dt)
+{
+	uint32_t h = dt % CLS_FOREIGN;
+	for (uint32_t p = 0; p < CLS_FOREIGN; p++) {
+		uint32_t cur = *(volatile uint32_t *) &tbl[h];
+		if (cur == dt) return h;
+		if (cur == TBL_EMPTY) {
+			cur = atomicCAS(&tbl[h], TBL_EMPTY, dt);
+			if (cur == TBL_EMPTY || cur == dt) return h;
+		}
+		h = (h + 1 == CLS_FOREIGN) ? 0 : h + 1;
+	}
+	return CLS_NONE;
+}
+
+__device__ __forceinline__ uint32_t class_find(const uint32_t *tbl, uint32_t dt)
+{
+	uint32_t h = dt % CLS_FOREIGN;
+	for (uint32_t p = 0; p < CLS_FOREIGN; p++) {
+		if (tbl[h] == dt) return h;
+		h = (h + 1 == CLS_FOREIGN) ? 0 : h + 1;
+	}
+	return CLS_NONE;
+}
+
+/* 16-byte asynchronous copy global -> shared (cp.async, bypassing L1). */
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+	const uint32_t sa = (uint32_t) __cvta_generic_to_shared(smem);
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16;"
+		:: "r"(sa), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit()
+{
+	asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+	asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+/* ctr[key] += 1 for every calling lane, one atomic per distinct key per
+ * warp; returns the counter's value before this lane's increment. */
+__device__ __forceinline__ uint32_t warp_agg_add(uint32_t *ctr, uint32_t key)
+{
+	const uint32_t act = __activemask();
+	const uint32_t peers = __match_any_sync(act, key);
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t leader = __ffs(peers) - 1;
+	uint32_t base = 0;
+	if (lane == leader) base = atomicAdd(&ctr[key], (uint32_t) __popc(peers));
+	base = __shfl_sync(peers, base, leader);
+	return base + __popc(peers & ((1u << lane) - 1));
+}
+
+/* Canonical order of the agents of one destination cell (x, y): by source
+ * cell, then by rank in the source cell's list. */
+__device__ __forceinline__ int64_t order_key(uint32_t rec, uint32_t x,
+	uint32_t y, uint32_t gx, uint32_t gy)
+{
+	const int32_t off = src_offset((rec >> REC_DIR_SHIFT) & 7u, x, y, gx, gy);
+	return (int64_t) off * 65536 + (rec >> REC_RANK_SHIFT);
+}
+
+/* Exclusive scan of one value per thread over the NT threads of the CTA;
+ * the total goes to *total. */
+__device__ __forceinline__ uint32_t step_excl_scan(uint32_t v, uint32_t *total)
+{
+	__shared__ uint32_t ws[NT / 32];
+	const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	uint32_t x = v;
+#pragma unroll
+	for (int o = 1; o < 32; o <<= 1) {
+		const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+		if (lane >= (uint32_t) o) x += y;
+	}
+	if (lane == 31) ws[wid] = x;
+	__syncthreads();
+	uint32_t before = 0, all = 0;
+#pragma unroll
+	for (uint32_t q = 0; q < NT / 32; q++) {
+		const uint32_t c = ws[q];
+		if (q < wid) before += c;
+		all += c;
+	}
+	*total = all;
+	__syncthreads();
+	return before + x - v;
+}
+
+/* One CTA per tile of CPT * NT cells.
+ *   ACT:  the act of iteration t of the tile's agents (gathered from its
+ *         inbox of parity t) and the move of iteration t + 1 of its
+ *         survivors and newborns into the group buffer of parity t + 1.
+ *   !ACT: the move of iteration 1 of a freshly initialised run's agents,
+ *         read cell-sorted from kS/vS at the tile offsets.
+ * Phases (ACT): gather; counting sort by cell with each multi-agent cell's
+ * list put in canonical order; B draws; C actions (as the sort pipeline's
+ * act); E0 output offsets and stats; E1 move draws and per-class counts;
+ * one warp allocates the tile's groups and posts them to the destination
+ * tiles' inboxes; E2 records into the groups; per-tile stats. */
+template <int CPT, bool ACT>
+__global__ void __launch_bounds__(NT, 8) k_step(WorldDev w,
+	const uint32_t *__restrict__ kS, const uint32_t *__restrict__ vS,
+	uint32_t tile0, uint32_t out_base)
+{
+	extern __shared__ __align__(16) uint32_t sm[];
+	uint32_t *sk = sm, *sv = sm + w.act_cap, *sp = sv + w.act_cap,
+		*sd = sp + w.act_cap, *sperm = sd + w.act_cap;
+	uint32_t *scnt = sperm + w.act_cap;                 /* CPT * NT */
+	uint16_t *sgrass = reinterpret_cast<uint16_t *>(scnt + CPT * NT);
+	__shared__ uint32_t s_tbl[CLS_FOREIGN];
+	__shared__ uint32_t s_ccnt[NCLS + 1], s_cpos[NCLS + 1];   /* + a discard slot */
+	__shared__ uint32_t s_xbase, s_fail;
+
+	const uint32_t tid = threadIdx.x, lane = tid & 31;
+	const uint32_t tile = tile0 + blockIdx.x;
+	const uint32_t c0 = tile << w.log_tile;
+	/* loads that depend on nothing, issued first: the tile's grass (async
+	 * copy into shared memory), both parities' inboxes (every warp reads
+	 * its own copy: no barrier before the gather), the tile's dense input
+	 * base */
+	uint32_t in_n0 = 0, in_n1 = 0, dbase_t = 0;
+	uint2 in_e0 = make_uint2(0u, 0u), in_e1 = make_uint2(0u, 0u);
+	if (ACT) {
+		const uint4 *src = reinterpret_cast<const uint4 *>(w.grass + c0);
+		for (uint32_t q = tid; q < CPT * NT / 8; q += NT)
+			cp_async16(reinterpret_cast<uint4 *>(sgrass) + q, src + q);
+		cp_async_commit();
+		const size_t ib0 = tile, ib1 = (size_t) w.n_tiles + tile;
+		in_n0 = w.inbox_n[ib0];
+		in_n1 = w.inbox_n[ib1];
+		in_e0 = w.inbox[ib0 * IBX + lane];
+		in_e1 = w.inbox[ib1 * IBX + lane];
+		dbase_t = w.dbase[tile];
+	}
+	const uint32_t g = w.ctr->giter + 1;
+	const uint32_t pin = g & 1, pout = ACT ? (g + 1) & 1 : g & 1;
+	const RunDev &run = w.runs[w.tile_run[tile]];
+	const uint32_t t = g - run.start_giter;
+	if (ACT && !run_live(run, t)) {
+		cp_async_wait_all();
+		/* finished run or free tile space: nothing survives, no stats */
+		if (tid == 0) w.inbox_n[(size_t) pin * w.n_tiles + tile] = 0;
+		if (tid < 8) w.part[(size_t) tile * 8 + tid] = 0;
+		return;
+	}
+	const uint32_t tmove = ACT ? t + 1 : t;
+	const bool live_move = run_live(run, tmove);
+	const uint32_t seed_lo = run.seed_lo, seed_hi = run.seed_hi;
+	const uint32_t lt0 = c0 - run.cbase;          /* run-local index of the tile start */
+	const uint32_t lcmask = (1u << w.log_tile) - 1;
+	if (tid < CLS_FOREIGN) s_tbl[tid] = TBL_EMPTY;
+	if (tid <= NCLS) s_ccnt[tid] = 0;
+	if (tid == NCLS) s_cpos[NCLS] = 0;
+	/* per-cell counters, transposed: cell c at SLOT(c) = (c % CPT) * NT +
+	 * c / CPT, so no two threads of a warp share a bank */
+#define SLOT(c) ((((c) % CPT) * NT) + (c) / CPT)
+	if (ACT) {
+#pragma unroll
+		for (int q = 0; q < CPT; q++) scnt[q * NT + tid] = 0;
+	}
+
+	/* ---- inputs ---- */
+	uint32_t m, a0 = 0;
+	uint32_t grp_start = 0, grp_pref = 0, nin = 0;   /* this lane's inbox group */
+	if (ACT) {
+		/* entries past the count are stale and ignored */
+		nin = min(pin ? in_n1 : in_n0, IBX);
+		uint2 e = pin ? in_e1 : in_e0;
+		if (lane >= nin) e = make_uint2(0u, 0u);
+		const uint32_t c = (e.y & GROUP_GRAVE) ? 0u : e.y;
+		uint32_t x = c;
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1) {
+			const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+			if (lane >= (uint32_t) o) x += y;
+		}
+		grp_start = e.x;
+		grp_pref = x - c;
+		m = __shfl_sync(0xffffffffu, x, 31);
+	} else {
+		a0 = w.tile_off[tile];
+		m = w.tile_off[tile + 1] - a0;
+	}
+	const bool in_smem = m <= w.act_cap;
+	if (!in_smem) {
+		/* crowded tile: its arrays go to global scratch (3 m slots: the
+		 * permutation, then the output map and the move directions) */
+		if (tid == 0) {
+			const uint32_t b = atomicAdd(&w.ctr->xtop, 3 * m);
+			s_fail = (uint64_t) b + 3ull * m > w.cap;
+			if (s_fail) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
+			s_xbase = b;
+		}
+	}
+	__syncthreads();
+	if (!in_smem && s_fail) {
+		if (ACT) cp_async_wait_all();
+		if (tid < 8) w.part[(size_t) tile * 8 + tid] = 0;
+		return;
+	}
+	uint32_t *UK, *UV, *PERM, *LK, *LV;
+	if (in_smem) {
+		UK = sk; UV = sv; PERM = sperm; LK = sp; LV = sd;
+	} else {
+		const uint32_t xb = s_xbase;
+		UK = w.scratch_prio + xb; UV = w.scratch_kid + xb;
+		PERM = w.scratch_perm + xb;
+		LK = w.scratch_key + xb; LV = w.scratch_val + xb;
+	}
+	uint32_t *LP = UK, *LD = UV;      /* priorities / dice, then offsets / kids */
+
+	const uint32_t cell0 = tid * CPT;
+	uint32_t eats = 0;
+	if (!ACT) {
+		for (uint32_t j = tid; j < m; j += NT) {
+			LK[j] = kS[a0 + j] - c0;
+			LV[j] = vS[a0 + j];
+		}
+		__syncthreads();
+	} else {
+		/* gather the tile's groups and count agents per cell: item j comes
+		 * from the last group whose prefix is <= j (groups with equal
+		 * prefixes before it are empty), found by a binary search over
+		 * the lanes' group prefixes; two items in flight per thread */
+		const uint32_t *kGi = pin ? w.kG1 : w.kG0;
+		const uint32_t *vGi = pin ? w.vG1 : w.vG0;
+		const uint32_t m_up = (m + NT - 1) / NT * NT;   /* warp-uniform trip count */
+		for (uint32_t j0 = tid; j0 < m_up; j0 += 2 * NT) {
+			uint32_t src[2];
+#pragma unroll
+			for (int u = 0; u < 2; u++) {
+				const uint32_t j = j0 + u * NT;
+				uint32_t lo = 0, hi = max(nin, 1u);     /* last q with pref <= j */
+#pragma unroll
+				for (int step = 0; step < 5; step++) {
+					const uint32_t mid = (lo + hi) >> 1;
+					const uint32_t pm = __shfl_sync(0xffffffffu, grp_pref, mid);
+					if (hi - lo > 1) {
+						if (pm <= j) lo = mid; else hi = mid;
+					}
+				}
+				src[u] = __shfl_sync(0xffffffffu, grp_start, lo)
+					+ (j - __shfl_sync(0xffffffffu, grp_pref, lo));
+			}
+			uint32_t kk[2], vv[2];
+#pragma unroll
+			for (int u = 0; u < 2; u++) {
+				if (j0 + u * NT < m) {
+					kk[u] = kGi[src[u]];
+					vv[u] = vGi[src[u]];
+				}
+			}
+#pragma unroll
+			for (int u = 0; u < 2; u++) {
+				const uint32_t j = j0 + u * NT;
+				if (j < m) {
+					UK[j] = kk[u];
+					UV[j] = vv[u];
+					atomicAdd(&scnt[SLOT(kk[u] & lcmask)], 1u);
+				}
+			}
+		}
+		uint64_t multi = 0;   /* this thread's cells holding two or more agents */
+		__syncthreads();
+		if (tid == 0) w.inbox_n[(size_t) pin * w.n_tiles + tile] = 0;
+		{
+			uint32_t loc = 0;
+#pragma unroll
+			for (int q = 0; q < CPT; q++) {
+				const uint32_t c = scnt[q * NT + tid];
+				loc += c;
+				if (c > 1) multi |= 1ull << q;
+			}
+			uint32_t tot;
+			uint32_t run_start = step_excl_scan(loc, &tot);
+#pragma unroll
+			for (int q = 0; q < CPT; q++) {
+				const uint32_t c = scnt[q * NT + tid];
+				scnt[q * NT + tid] = run_start;
+				run_start += c;
+			}
+		}
+		__syncthreads();
+		for (uint32_t j = tid; j < m; j += NT)
+			PERM[atomicAdd(&scnt[SLOT(UK[j] & lcmask)], 1u)] = j;
+		__syncthreads();
+		/* scnt[SLOT(c)] is now the end of cell c; put each multi-agent
+		 * cell's list in canonical order */
+		while (multi) {
+			const int q = __ffsll((long long) multi) - 1;
+			multi &= multi - 1;
+			const uint32_t c = cell0 + q;
+			const uint32_t b = c ? scnt[SLOT(c - 1)] : 0, e = scnt[SLOT(c)];
+			const uint32_t lr = lt0 + c;
+			const uint32_t y = fastdiv_div(lr, run.gxdiv), x = lr - y * run.gx;
+			for (uint32_t i = b + 1; i < e; i++) {
+				const uint32_t xj = PERM[i];
+				const int64_t kx = order_key(UK[xj], x, y, run.gx, run.gy);
+				uint32_t h = i;
+				while (h > b && order_key(UK[PERM[h - 1]], x, y, run.gx, run.gy) > kx) {
+					PERM[h] = PERM[h - 1];
+					h--;
+				}
+				PERM[h] = xj;
+			}
+		}
+#undef SLOT
+		__syncthreads();
+		for (uint32_t i = tid; i < m; i += NT) {
+			const uint32_t j = PERM[i];
+			LK[i] = UK[j] & lcmask;
+			LV[i] = UV[j];
+		}
+		__syncthreads();
+		/* B: draws of every agent */
+		for (uint32_t j = tid; j < m; j += NT) {
+			const uint32_t lc = LK[j];
+			uint32_t k = 0;
+			while (k < j && LK[j - k - 1] == lc) k++;
+			u4 r = rng(seed_lo, seed_hi, lt0 + lc, t, STREAM_ACT, k);
+			LP[j] = r.x;
+			LD[j] = draw(r.y, 100);
+		}
+		cp_async_wait_all();
+		__syncthreads();
+		/* C: actions, one thread per occupied cell (its first agent's) */
+		ActParams ap;
+		ap.sheep_gain = run.sheep_gain; ap.sheep_thr = run.sheep_thr;
+		ap.sheep_prob = run.sheep_prob; ap.wolves_gain = run.wolves_gain;
+		ap.wolves_thr = run.wolves_thr; ap.wolves_prob = run.wolves_prob;
+		ap.restart = run.restart;
+		const uint16_t t16 = (uint16_t) t;
+		for (uint32_t j = tid; j < m; j += NT) {
+			const uint32_t lc = LK[j];
+			if (j > 0 && LK[j - 1] == lc) continue;
+			uint32_t e = j + 1;
+			while (e < m && LK[e] == lc) e++;
+			const int32_t dd = (int16_t) (uint16_t) (sgrass[lc] - t16);
+			uint32_t gq = dd > 0 ? (uint32_t) dd : 0u;
+			const uint32_t g0 = gq;
+			act_cell(j, e, LV, LP, LD, ap, gq);
+			if (gq != g0) {
+				w.grass[c0 + lc] = (uint16_t) (t16 + (uint16_t) ap.restart);
+				eats++;
+			}
+		}
+		__syncthreads();
+	}
+
+	/* ---- E0: output offsets (each survivor, then its newborn), stats,
+	 * and the output -> agent map OUTJ (agent index | newborn << 15) ---- */
+	const uint32_t ch = (m + NT - 1) / NT;
+	const uint32_t ja = min(tid * ch, m), jb = min(ja + ch, m);
+	uint32_t cnt = 0, sheep = 0, wolves = 0;
+	uint64_t sen = 0, wen = 0;
+	if (ACT) {
+		for (uint32_t j = ja; j < jb; j++) {
+			const uint32_t v = LV[j], kd = LD[j];
+			const uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
+			if (en) {
+				cnt++;
+				if (tb) { wolves++; wen += en; } else { sheep++; sen += en; }
+			}
+			if (kd) {
+				cnt++;
+				if (tb) { wolves++; wen += kd; } else { sheep++; sen += kd; }
+			}
+		}
+	}
+	uint32_t total = m;
+	/* output map: 16-bit entries in the permutation's shared array (2 m
+	 * <= 2 act_cap), 32-bit ones in a crowded tile's scratch; directions:
+	 * bytes in the cell counters (2 m <= 4 T) or after the map */
+	uint16_t *OUTJ16 = reinterpret_cast<uint16_t *>(PERM);
+	uint32_t *OUTJ32 = PERM;
+	uint8_t *DIR = in_smem ? reinterpret_cast<uint8_t *>(scnt)
+		: reinterpret_cast<uint8_t *>(PERM + 2 * m);
+	if (ACT) {
+		uint32_t o = step_excl_scan(cnt, &total);
+		for (uint32_t j = ja; j < jb; j++) {
+			LP[j] = o;
+			if (LV[j] & ENERGY_MASK) {
+				if (in_smem) OUTJ16[o] = (uint16_t) j; else OUTJ32[o] = j;
+				o++;
+			}
+			if (LD[j]) {
+				if (in_smem) OUTJ16[o] = (uint16_t) (j | 0x8000u);
+				else OUTJ32[o] = j | 0x80000000u;
+				o++;
+			}
+		}
+		__syncthreads();
+	}
+	/* the tile's slots in the group buffer: twice its dense input base
+	 * (at most two outputs per input), or after out_base for a first move */
+	const uint32_t gb = ACT ? 2 * dbase_t : out_base + a0;
+
+	/* output o: its agent j, whether it is a newborn, its energy and rank
+	 * in its cell's new list */
+	auto output = [&](uint32_t o, uint32_t &j, uint32_t &nb, uint32_t &en,
+		uint32_t &rank) {
+		if (ACT) {
+			if (in_smem) {
+				const uint32_t u = OUTJ16[o];
+				j = u & 0x7fffu;
+				nb = u >> 15;
+			} else {
+				const uint32_t u = OUTJ32[o];
+				j = u & 0x7fffffffu;
+				nb = u >> 31;
+			}
+		} else {
+			j = o;
+			nb = 0;
+		}
+		const uint32_t lc = LK[j];
+		uint32_t f = j;
+		while (f > 0 && LK[f - 1] == lc) f--;
+		rank = o - (ACT ? LP[f] : f);
+		en = nb ? LD[j] : (LV[j] & ENERGY_MASK);
+	};
+
+	/* ---- E1: move draws of the outputs, per-class counts ---- */
+	bool bad = false;
+	for (uint32_t o = tid; o < total; o += NT) {
+		uint32_t j, nb, en, rank;
+		output(o, j, nb, en, rank);
+		const uint32_t lc = LK[j];
+		uint32_t code, cls;
+		if (!live_move) {
+			code = DIR_PARKED;
+			cls = CLS_GRAVE;
+		} else if (en <= 1) {
+			code = DIR_DEAD;
+			cls = CLS_GRAVE;
+		} else {
+			const u4 r = rng(seed_lo, seed_hi, lt0 + lc, tmove, STREAM_MOVE, rank);
+			code = draw(r.x, 5);
+			const uint32_t dt = (run.cbase + move_dir(run, lt0 + lc, code)) >> w.log_tile;
+			cls = dt == tile ? CLS_OWN : class_insert(s_tbl, dt);
+		}
+		DIR[o] = (uint8_t) code;
+		if (cls == CLS_NONE || rank > REC_RANK_MAX) {
+			bad = true;
+			cls = NCLS;                      /* counted nowhere */
+		}
+		warp_agg_add(s_ccnt, cls);
+	}
+	if (bad) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
+	__syncthreads();
+
+	/* ---- the tile's groups: one per class, laid out in class order
+	 * from its slots ---- */
+	uint32_t my_c = 0, my_start = 0;
+	if (tid < 32) {
+		my_c = s_ccnt[lane];
+		uint32_t x = my_c;
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1) {
+			const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+			if (lane >= (uint32_t) o) x += y;
+		}
+		const bool fail = (uint64_t) gb + total > 3ull * w.cap;
+		if (lane == 0) {
+			s_fail = fail;
+			if (fail) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
+		}
+		my_start = gb + x - my_c;
+		s_cpos[lane] = my_start;
+	}
+	__syncthreads();
+
+	if (!s_fail) {
+		/* the groups are posted to their destination tiles' inboxes by
+		 * warp 0 while the records are written */
+		uint32_t slot = IBX;
+		size_t ib = 0;
+		if (tid < 32 && my_c) {
+			const uint32_t dt = lane < CLS_FOREIGN ? s_tbl[lane] : tile;
+			ib = (size_t) pout * w.n_tiles + dt;
+			slot = atomicAdd(&w.inbox_n[ib], 1u);
+		}
+		/* ---- E2: records into the groups ---- */
+		uint32_t *kGo = pout ? w.kG1 : w.kG0;
+		uint32_t *vGo = pout ? w.vG1 : w.vG0;
+		for (uint32_t o = tid; o < total; o += NT) {
+			uint32_t j, nb, en, rank;
+			output(o, j, nb, en, rank);
+			const uint32_t lc = LK[j];
+			const uint32_t tb = LV[j] & TYPE_BIT;
+			const uint32_t code = DIR[o];
+			uint32_t key, val, cls;
+			if (code >= DIR_PARKED) {
+				cls = CLS_GRAVE;
+				key = lc | (code << REC_DIR_SHIFT) | (rank << REC_RANK_SHIFT);
+				val = tb | en;
+			} else {
+				const uint32_t dg = run.cbase + move_dir(run, lt0 + lc, code);
+				const uint32_t dt = dg >> w.log_tile;
+				cls = dt == tile ? CLS_OWN : class_find(s_tbl, dt);
+				key = (dg & lcmask) | (code << REC_DIR_SHIFT) | (rank << REC_RANK_SHIFT);
+				val = tb | (en - 1);
+			}
+			if (cls == CLS_NONE || rank > REC_RANK_MAX) cls = NCLS;
+			const uint32_t pos = warp_agg_add(s_cpos, cls);
+			if (cls != NCLS) {
+				kGo[pos] = key;
+				vGo[pos] = val;
+			}
+		}
+		if (tid < 32 && my_c) {
+			if (slot < IBX)
+				w.inbox[ib * IBX + slot] = make_uint2(my_start,
+					my_c | (lane == CLS_GRAVE ? GROUP_GRAVE : 0u));
+			else
+				atomicOr(&w.ctr->err, ERRF_OVERFLOW);
+		}
+	}
+
+	/* ---- per-tile partial stats (ACT); the tile's eating events go to the
+	 * run's regrowth histogram slot of iteration t + restart ---- */
+	if (ACT) {
+		__shared__ uint64_t red[5][NT / 32];
+		const uint32_t wid = tid >> 5;
+		const uint32_t sw = warp_sum(sheep | (wolves << 16));
+		const uint32_t ew = warp_sum(eats);
+		const uint64_t se = warp_sum(sen), we = warp_sum(wen);
+		if (lane == 0) {
+			red[0][wid] = sw & 0xffffu;
+			red[1][wid] = sw >> 16;
+			red[2][wid] = ew;
+			red[3][wid] = se;
+			red[4][wid] = we;
+		}
+		__syncthreads();
+		if (tid < 5) {
+			uint64_t sum = 0;
+			for (uint32_t q = 0; q < NT / 32; q++) sum += red[tid][q];
+			if (tid == 2) {
+				if (sum)
+					atomicAdd(&w.fring[run.fbase + (t + run.restart) % (run.restart + 1)],
+						(uint32_t) sum);
+				w.part[(size_t) tile * 8 + 2] = 0;
+				w.part[(size_t) tile * 8 + 5] = 0;
+			} else {
+				w.part[(size_t) tile * 8 + tid] = sum;
+			}
+		}
+	}
+}
+
+template <bool ACT>
+cudaError_t launch_step(const WorldDev &w, const LaunchCfg &lc,
+	const uint32_t *k, const uint32_t *v, uint32_t first, uint32_t count,
+	uint32_t out_base, cudaStream_t s)
+{
+	const uint32_t T = 1u << w.log_tile;
+	const size_t smem = (size_t) w.act_cap * 5 * sizeof(uint32_t)
+		+ (size_t) T * (sizeof(uint32_t) + sizeof(uint16_t));
+	(void) lc;
+	switch (T / NT) {
+	case 8: k_step<8, ACT><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
+	case 16: k_step<16, ACT><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
+	case 32: k_step<32, ACT><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
+	default: k_step<64, ACT><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
+	}
+	return cudaGetLastError();
+}
+
+template <int CPT>
+cudaError_t set_step_limit(size_t bytes)
+{
+	cudaError_t e = cudaFuncSetAttribute(k_step<CPT, true>,
+		cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+	if (e != cudaSuccess) return e;
+	return cudaFuncSetAttribute(k_step<CPT, false>,
+		cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+}
+
+} /* namespace */
+
+cudaError_t enqueue_iteration_fused(const WorldDev &w, const LaunchCfg &lc,
+	cudaStream_t s, const cudaEvent_t *marks)
+{
+	/* marks (optional, 3 events): before the act, after it, after the
+	 * finish */
+	if (marks) cudaEventRecord(marks[0], s);
+	cudaError_t e = launch_step<true>(w, lc, nullptr, nullptr, 0, w.n_tiles, 0, s);
+	if (e != cudaSuccess) return e;
+	if (marks) cudaEventRecord(marks[1], s);
+	e = launch_finish_fused(w, lc, s);
+	if (marks) cudaEventRecord(marks[2], s);
+	return e;
+}
+
+cudaError_t enqueue_move_groups(const WorldDev &w, const LaunchCfg &lc,
+	const uint32_t *k, const uint32_t *v, uint32_t first, uint32_t count,
+	uint32_t out_base, cudaStream_t s)
+{
+	if (count == 0) return cudaSuccess;
+	return launch_step<false>(w, lc, k, v, first, count, out_base, s);
+}
+
+cudaError_t set_step_smem_limits(size_t bytes)
+{
+	cudaError_t e = set_step_limit<8>(bytes);
+	if (e == cudaSuccess) e = set_step_limit<16>(bytes);
+	if (e == cudaSuccess) e = set_step_limit<32>(bytes);
+	if (e == cudaSuccess) e = set_step_limit<64>(bytes);
+	return e;
+}
+
+} /* namespace pp */

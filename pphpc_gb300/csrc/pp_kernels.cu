@@ -27,42 +27,13 @@
  */
 #include "pp_kernels.cuh"
 #include "pp_block.cuh"
+#include "pp_act.cuh"
 
 namespace pp {
 
 /* ------------------------------------------------------------------ */
 /* Move                                                                */
 /* ------------------------------------------------------------------ */
-
-/* Energy loss, death and toroidal random walk of one agent of rank k in
- * its cell (pp_gpu.cl:756-819; per-row wrap as there). */
-__device__ __forceinline__ void move_one(const RunDev &run, uint32_t key,
-	uint32_t val, uint32_t k, uint32_t t, uint32_t dead_key,
-	uint32_t &nk, uint32_t &nv)
-{
-	uint32_t e = val & ENERGY_MASK;
-	if (e <= 1) {
-		nk = dead_key;
-		nv = val & TYPE_BIT;
-		return;
-	}
-	uint32_t lc = key - run.cbase;
-	u4 r = rng(run.seed_lo, run.seed_hi, lc, t, STREAM_MOVE, k);
-	uint32_t dir = draw(r.x, 5);
-	uint32_t y = fastdiv_div(lc, run.gxdiv);
-	uint32_t x = lc - y * run.gx;
-	if (dir == 1) x = (x + 1 == run.gx) ? 0 : x + 1;
-	else if (dir == 2) x = (x == 0) ? run.gx - 1 : x - 1;
-	else if (dir == 3) y = (y + 1 == run.gy) ? 0 : y + 1;
-	else if (dir == 4) y = (y == 0) ? run.gy - 1 : y - 1;
-	nk = run.cbase + y * run.gx + x;
-	nv = val - 1;
-}
-
-__device__ __forceinline__ bool run_live(const RunDev &run, uint32_t t)
-{
-	return run.active && t >= 1 && t <= run.iters;
-}
 
 /* One warp per tile region: the tile's agents (cell-sorted lists) from the
  * region buffer. MOVE: the move of every agent (draw keyed by cell and
@@ -193,108 +164,6 @@ __global__ void k_offsets(const uint32_t *keys, const uint32_t *n_dev,
 /* Act                                                                 */
 /* ------------------------------------------------------------------ */
 
-/* Model parameters the actions need, held in registers. */
-struct ActParams {
-	uint32_t sheep_gain, sheep_thr, sheep_prob;
-	uint32_t wolves_gain, wolves_thr, wolves_prob;
-	uint32_t restart;
-};
-
-/* Actions of the agents of one cell, entries [p, e) of the tile's agent
- * list in cell-list order, in increasing (priority, rank) order; on entry
- * LP[j] / LD[j] hold the priority and the dice of the agent of rank j - p,
- * drawn from Philox({cell, t, ACT, rank}). This is the sequential semantics
- * of pp_cpu.cl:640-848 (wolves eat the first not-yet-eaten sheep of the
- * cell; a sheep acts only if not eaten before its turn; the first acting
- * sheep takes live grass; every acting agent may reproduce) in closed form:
- * the k-th wolf eats the k-th sheep, and a sheep acts iff the wolves before
- * it are no more than the sheep before it.
- * On return LV[j] holds type | final energy (energy 0 = eaten) and LD[j]
- * the newborn's energy (0 = none). */
-__device__ __forceinline__ void act_cell(uint32_t p, uint32_t e,
-	uint32_t *LV, const uint32_t *LP, uint32_t *LD, const ActParams &ap,
-	uint32_t &g)
-{
-	if (e - p == 1) {
-		/* alone in its cell: a sheep acts and is not eaten, a wolf finds
-		 * no sheep */
-		const uint32_t v = LV[p], tb = v & TYPE_BIT;
-		uint32_t en = v & ENERGY_MASK, thr, prob;
-		if (tb) {
-			thr = ap.wolves_thr;
-			prob = ap.wolves_prob;
-		} else {
-			if (g == 0) {
-				g = ap.restart;
-				en += ap.sheep_gain;
-			}
-			thr = ap.sheep_thr;
-			prob = ap.sheep_prob;
-		}
-		const uint32_t kid = (en > thr && LD[p] < prob) ? en >> 1 : 0;
-		LV[p] = tb | (en - kid);
-		LD[p] = kid;
-		return;
-	}
-	uint32_t S = 0, W = 0;
-	for (uint32_t j = p; j < e; j++) {
-		if (LV[j] & TYPE_BIT) W++;
-		else S++;
-	}
-	uint32_t sb = 0, wb = 0;
-	uint32_t lp = 0;
-	uint32_t ls = 0xffffffffu; /* none selected yet */
-	const uint32_t m = e - p;
-	for (uint32_t step = 0; step < m; step++) {
-		uint32_t best = p;
-		if (m > 1) {
-			uint32_t bp = 0xffffffffu;
-			bool found = false;
-			for (uint32_t j = p; j < e; j++) {
-				uint32_t pj = LP[j];
-				bool after = (ls == 0xffffffffu) || pj > lp
-					|| (pj == lp && j > ls);
-				if (after && (!found || pj < bp)) {
-					best = j;
-					bp = pj;
-					found = true;
-				}
-			}
-		}
-		uint32_t v = LV[best];
-		uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
-		uint32_t dice = LD[best];
-		bool acts, eaten = false;
-		uint32_t thr, prob;
-		if (tb) {
-			if (wb < S) en += ap.wolves_gain;
-			wb++;
-			acts = true;
-			thr = ap.wolves_thr;
-			prob = ap.wolves_prob;
-		} else {
-			acts = wb <= sb;
-			eaten = sb < W;
-			sb++;
-			if (acts && g == 0) {
-				g = ap.restart;
-				en += ap.sheep_gain;
-			}
-			thr = ap.sheep_thr;
-			prob = ap.sheep_prob;
-		}
-		uint32_t kid = 0;
-		if (acts && en > thr && dice < prob) {
-			kid = en >> 1;
-			en -= kid;
-		}
-		LV[best] = tb | (eaten ? 0u : en);
-		LD[best] = kid;
-		lp = LP[best];
-		ls = best;
-	}
-}
-
 /* First index in a[0, m) with a[i] >= x. */
 __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *a,
 	uint32_t m, uint32_t x)
@@ -360,47 +229,6 @@ __device__ uint32_t warp_lookback(uint64_t *lb, uint32_t tile, uint32_t agg,
 	if (lane == 0)
 		st_release_u64(&lb[tile], lb_pack(epoch, LB_FLAG_PREFIX, acc + agg));
 	return acc;
-}
-
-struct StatAcc {
-	uint32_t sheep, wolves, galive;
-	uint64_t sen, wen, gen;
-	__device__ void zero() { sheep = wolves = galive = 0; sen = wen = gen = 0; }
-};
-
-/* Block-reduce the per-thread stats into out[0..5] (u64, thread f writes
- * field f). Must be called by all threads of the block. */
-__device__ void block_stats(const StatAcc &a, uint64_t *out)
-{
-	__shared__ uint64_t red[6][ACT_THREADS / 32];
-	uint64_t v[6] = {a.sheep, a.wolves, a.galive, a.sen, a.wen, a.gen};
-	const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-	for (int f = 0; f < 6; f++) {
-		v[f] = warp_sum(v[f]);
-		if (lane == 0) red[f][wid] = v[f];
-	}
-	__syncthreads();
-	if (threadIdx.x < 6) {
-		uint64_t s = 0;
-		for (uint32_t q = 0; q < ACT_THREADS / 32; q++) s += red[threadIdx.x][q];
-		out[threadIdx.x] = s;
-	}
-	__syncthreads();
-}
-
-__device__ __forceinline__ void stats_atomic_add(PPStatistics *dst,
-	uint32_t f, uint64_t s)
-{
-	if (!s) return;
-	switch (f) {
-	case 0: atomicAdd(&dst->sheep, (uint32_t) s); break;
-	case 1: atomicAdd(&dst->wolves, (uint32_t) s); break;
-	case 2: atomicAdd(&dst->grass, (uint32_t) s); break;
-	case 3: atomicAdd((unsigned long long *) &dst->sheep_en, s); break;
-	case 4: atomicAdd((unsigned long long *) &dst->wolves_en, s); break;
-	default: atomicAdd((unsigned long long *) &dst->grass_en, s); break;
-	}
 }
 
 /* One CTA per tile of CPT * 256 cells (tiles do not depend on each other).
@@ -633,7 +461,7 @@ __global__ void __launch_bounds__(ACT_THREADS, 5) k_act(WorldDev w,
  *   total above the agent pool raises ERRF_OVERFLOW (pp_gpu.c:847-852);
  *   the last CTA resets the per-launch counters (FULL: advances the
  *   iteration, clears the histograms and the next stats row). */
-template <bool FULL>
+template <bool FULL, bool FUSED>
 __global__ void __launch_bounds__(256) k_finish(WorldDev w)
 {
 	__shared__ uint32_t s_chunk, s_last, s_base;
@@ -700,11 +528,32 @@ __global__ void __launch_bounds__(256) k_finish(WorldDev w)
 			f[t % fs] = 0;
 		}
 	}
-	/* dense bases of the regions */
+	/* dense bases: of the regions (sort pipeline), or of the next act's
+	 * inputs, counted from the groups posted to each tile's inbox (fused
+	 * pipeline; the next act writes its groups at twice its base) */
+	const uint32_t pnext = FULL ? (g + 1) & 1 : g & 1;
+	uint32_t all = 0;    /* fused: every posted record (dead ones too) */
+	auto tile_count = [&](uint32_t tl) -> uint32_t {
+		if (!FUSED) return w.rcnt[tl];
+		const size_t ib = (size_t) pnext * w.n_tiles + tl;
+		const uint32_t n = min(w.inbox_n[ib], IBX);
+		uint32_t c = 0;
+		for (uint32_t i = 0; i < n; i++) {
+			const uint32_t y = w.inbox[ib * IBX + i].y;
+			c += (y & GROUP_GRAVE) ? 0u : y;
+			all += y & ~GROUP_GRAVE;
+		}
+		return c;
+	};
 	const uint32_t tpt = (per + blockDim.x - 1) / blockDim.x;
 	const uint32_t ta = min(t0 + threadIdx.x * tpt, t1), tb = min(ta + tpt, t1);
 	uint32_t local = 0;
-	for (uint32_t tl = ta; tl < tb; tl++) local += w.rcnt[tl];
+	for (uint32_t tl = ta; tl < tb; tl++) local += tile_count(tl);
+	if (FUSED) {
+		/* the agent count after the act: all records, summed per CTA */
+		const uint32_t a = warp_sum(all);
+		if ((threadIdx.x & 31) == 0 && a) atomicAdd(&w.ctr->n_all, a);
+	}
 	uint32_t total;
 	const uint32_t excl = block_excl_scan(local, &total);
 	if (threadIdx.x < 32) {
@@ -715,13 +564,13 @@ __global__ void __launch_bounds__(256) k_finish(WorldDev w)
 	uint32_t run = s_base + excl;
 	for (uint32_t tl = ta; tl < tb; tl++) {
 		w.dbase[tl] = run;
-		run += w.rcnt[tl];
+		run += tile_count(tl);
 	}
 	if (chunk == gridDim.x - 1 && threadIdx.x == 0) {
 		const uint32_t n = s_base + total;
 		w.dbase[w.n_tiles] = n;
 		if (n > w.cap) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
-		w.ctr->n_agents = min(n, w.cap);
+		if (!FUSED) w.ctr->n_agents = min(n, w.cap);
 	}
 	__threadfence();
 	__syncthreads();
@@ -731,9 +580,15 @@ __global__ void __launch_bounds__(256) k_finish(WorldDev w)
 		if (done == gridDim.x - 1) {
 			__threadfence();
 			s_last = 1;
+			if (FUSED) {
+				const uint32_t n = ld_volatile_u32(&w.ctr->n_all);
+				if (n > w.cap) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
+				w.ctr->n_agents = min(n, w.cap);
+				w.ctr->n_all = 0;
+			}
 			if (FULL) {
 				w.ctr->giter = g;
-				w.ctr->act_ticket = 0;
+				w.ctr->xtop = 0;
 				for (int q = 0; q < 8; q++) w.ctr->sort_ticket[q] = 0;
 			}
 			w.ctr->seq = w.ctr->seq + 1;
@@ -918,8 +773,22 @@ cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
 	default: k_act<8><<<w.n_tiles, ACT_THREADS, act_smem, s>>>(w, ki, vi); break;
 	}
 	if (marks) cudaEventRecord(marks[3 + w.passes], s);
-	k_finish<true><<<lc.finish_blocks, 256, 0, s>>>(w);
+	k_finish<true, false><<<lc.finish_blocks, 256, 0, s>>>(w);
 	if (marks) cudaEventRecord(marks[4 + w.passes], s);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_finish_fused(const WorldDev &w, const LaunchCfg &lc,
+	cudaStream_t s)
+{
+	k_finish<true, true><<<lc.finish_blocks, 256, 0, s>>>(w);
+	return cudaGetLastError();
+}
+
+cudaError_t enqueue_fused_bases(const WorldDev &w, const LaunchCfg &lc,
+	cudaStream_t s)
+{
+	k_finish<false, true><<<lc.finish_blocks, 256, 0, s>>>(w);
 	return cudaGetLastError();
 }
 
@@ -980,7 +849,7 @@ cudaError_t enqueue_regions_from_sorted(const WorldDev &w, const LaunchCfg &lc,
 	if (b == 0) b = 1;
 	if (b > 4096) b = 4096;
 	k_regions_set<<<b, 256, 0, s>>>(w, first, count, base);
-	k_finish<false><<<lc.finish_blocks, 256, 0, s>>>(w);
+	k_finish<false, false><<<lc.finish_blocks, 256, 0, s>>>(w);
 	return cudaGetLastError();
 }
 

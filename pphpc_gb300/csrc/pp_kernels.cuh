@@ -38,6 +38,16 @@ struct WorldDev {
 	uint32_t sort_shift;      /* the sort orders key bits [sort_shift, key_bits) */
 	uint32_t act_cap;         /* agents per tile held in shared memory     */
 	uint32_t dead_key;        /* = n_tiles << log_tile                      */
+	/* fused pipeline: the state between iterations is, per parity, a group
+	 * buffer of moved agents (records, see pp_device.cuh) and per tile an
+	 * inbox listing the groups destined to it */
+	uint32_t *kG0, *vG0, *kG1, *vG1;   /* group buffers, 3 * cap slots each: the
+	                           act of tile t writes at 2 * dbase[t] (dbase =
+	                           dense base of its next-act inputs), admitted
+	                           runs' first moves from 2 * cap on */
+	uint2 *inbox;             /* [2][n_tiles][IBX]                          */
+	uint32_t *inbox_n;        /* [2][n_tiles]                               */
+	uint32_t fused;
 };
 
 struct LaunchCfg {
@@ -56,6 +66,24 @@ constexpr int ACT_THREADS = 256;
  * CUDA error code (cudaSuccess = 0). */
 cudaError_t enqueue_iteration(const WorldDev &w, const LaunchCfg &lc,
 	cudaStream_t s, const cudaEvent_t *marks = nullptr);
+
+/* One fused iteration: act+move (gather by destination tile), finish. */
+cudaError_t enqueue_iteration_fused(const WorldDev &w, const LaunchCfg &lc,
+	cudaStream_t s, const cudaEvent_t *marks = nullptr);
+
+/* Fused pipeline: the first move of the agents of tiles [first, first +
+ * count), cell-sorted in k/v (tile offsets in w.tile_off), into the group
+ * buffer the next act reads. */
+cudaError_t enqueue_move_groups(const WorldDev &w, const LaunchCfg &lc,
+	const uint32_t *k, const uint32_t *v, uint32_t first, uint32_t count,
+	uint32_t out_base, cudaStream_t s);
+
+/* Fused pipeline: dense bases of the next act's per-tile inputs (after a
+ * first move outside an iteration). */
+cudaError_t enqueue_fused_bases(const WorldDev &w, const LaunchCfg &lc,
+	cudaStream_t s);
+
+cudaError_t set_step_smem_limits(size_t bytes);
 
 /* Initialisation of a run: grass of its tiles; its initial agents in
  * creation order into k/v[base ..) (sorted by cell afterwards); the stats

@@ -80,18 +80,21 @@ extern "C" int pp_serve_create(const pp_serve_opts *opts, pp_server **out)
 	pp_server *srv = new (std::nothrow) pp_server();
 	if (!srv) return PP_OUT_OF_RESOURCES;
 	srv->opts = o;
-	/* Budget split: a cell costs ~2 B (grass) + 8 B/2048 (look-back) and an
-	 * agent slot 32 B (three key/value arrays and two scratch words) plus
-	 * 0.5 B of sort look-back. Cells are bounded by the 2^31 key space. */
+	/* Budget split: a tile costs 2 B per cell (grass) plus ~610 B of
+	 * per-tile tables (inboxes, offsets, partial stats), an agent slot 93 B
+	 * (three key/value arrays for sorting a new run's agents, two group
+	 * buffers of three slots per agent, five scratch words for crowded
+	 * tiles, sort look-back). Cells are bounded by the 2^31 key space. */
 	const uint32_t T = 2048;
+	const uint64_t tile_bytes = T * 2ull + 610;
 	uint64_t budget = o.mem_budget_bytes;
 	uint64_t cell_bytes = budget / 8;
-	uint64_t tiles = cell_bytes / (T * 2ull + 8);
+	uint64_t tiles = cell_bytes / tile_bytes;
 	uint64_t max_tiles = ((1ull << 31) / T) - 1;
 	if (tiles > max_tiles) tiles = max_tiles;
 	if (tiles < 1) tiles = 1;
-	uint64_t rest = budget - tiles * (T * 2ull + 8);
-	uint64_t cap = rest / 33;
+	uint64_t rest = budget > tiles * tile_bytes ? budget - tiles * tile_bytes : 0;
+	uint64_t cap = rest / 93;
 	if (cap > 0x7fffffffull) cap = 0x7fffffffull;
 	if (cap < 4096) cap = 4096;
 	WorldConfig cfg;

@@ -16,6 +16,7 @@
 #include <new>
 
 #include "pp_world.cuh"
+#include "pp_act.cuh"
 
 namespace pp {
 
@@ -150,6 +151,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	if (nruns_cap > 65535) return PP_INVALID_ARGS;
 
 	w_.cap = cfg.cap;
+	w_.fused = cfg.fused ? 1u : 0u;
 	w_.n_tiles = (uint32_t) tiles;
 	w_.log_tile = log_tile;
 	w_.nruns_cap = nruns_cap;
@@ -179,6 +181,9 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 		act_cap = pow2_ceil((uint32_t) (T * dens * 0.75) + 1);
 		act_cap = std::min<uint32_t>(std::max<uint32_t>(act_cap, 256), 4096);
 	}
+	/* the fused act keeps a byte per output (at most 2 act_cap) in the
+	 * tile's 4 T bytes of cell counters */
+	act_cap = std::min<uint32_t>(act_cap, 2 * T);
 	w_.act_cap = act_cap;
 
 	const size_t cap = cfg.cap;
@@ -189,7 +194,14 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	PP_AL(w_.kA, cap * 4); PP_AL(w_.vA, cap * 4);
 	PP_AL(w_.kB, cap * 4); PP_AL(w_.vB, cap * 4);
 	PP_AL(w_.kC, cap * 4); PP_AL(w_.vC, cap * 4);
-	PP_AL(w_.kR, 3 * cap * 4); PP_AL(w_.vR, 3 * cap * 4);
+	if (w_.fused) {
+		PP_AL(w_.kG0, 3 * cap * 4); PP_AL(w_.vG0, 3 * cap * 4);
+		PP_AL(w_.kG1, 3 * cap * 4); PP_AL(w_.vG1, 3 * cap * 4);
+		PP_AL(w_.inbox, (size_t) 2 * tiles * IBX * sizeof(uint2));
+		PP_AL(w_.inbox_n, (size_t) 2 * tiles * 4);
+	} else {
+		PP_AL(w_.kR, 3 * cap * 4); PP_AL(w_.vR, 3 * cap * 4);
+	}
 	PP_AL(w_.scratch_key, cap * 4); PP_AL(w_.scratch_val, cap * 4);
 	PP_AL(w_.scratch_prio, cap * 4); PP_AL(w_.scratch_kid, cap * 4);
 	PP_AL(w_.scratch_perm, cap * 4);
@@ -226,6 +238,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	PP_CK(cudaMemsetAsync(w_.ring, 0, (size_t) w_.ring_rows * nruns_cap * sizeof(PPStatistics), s_));
 	PP_CK(cudaMemsetAsync(w_.part, 0, (size_t) tiles * 8 * sizeof(uint64_t), s_));
 	PP_CK(cudaMemsetAsync(w_.fring, 0, std::max<uint64_t>(fsz, 1) * 4, s_));
+	if (w_.fused) PP_CK(cudaMemsetAsync(w_.inbox_n, 0, (size_t) 2 * tiles * 4, s_));
 
 	/* Run table and tile map. */
 	runs_h_.assign(nruns_cap, RunDev{});
@@ -251,6 +264,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	lc_.cpt = (int) (T / ACT_THREADS);
 	size_t act_smem = (size_t) act_cap * 20 + (size_t) T * 6;
 	PP_CK(set_act_smem_limits(act_smem));
+	PP_CK(set_step_smem_limits(act_smem));
 	int occ_sort = occupancy_sort((int) d);
 	if (occ_sort < 1) occ_sort = 1;
 	lc_.sort_blocks = sms * occ_sort;
@@ -269,13 +283,25 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 			runs[r].p.init_sheep, runs[r].p.init_wolves, s_));
 		if (rc) return rc;
 	}
-	rc = sort_into(base, w_.kR, w_.vR);
-	if (rc) return rc;
-	rc = cuda_status(enqueue_regions_from_sorted(w_, lc_, w_.kR, 0, (uint32_t) tiles, 0, s_));
-	if (rc) return rc;
+	uint32_t *sorted_v;
+	if (w_.fused) {
+		/* sorted into A; the first move of every agent into the group
+		 * buffer the first act reads */
+		rc = sort_into(base, w_.kA, w_.vA);
+		if (rc) return rc;
+		rc = place_sorted(base, 0, (uint32_t) tiles, 0);
+		if (rc) return rc;
+		sorted_v = w_.vA;
+	} else {
+		rc = sort_into(base, w_.kR, w_.vR);
+		if (rc) return rc;
+		rc = cuda_status(enqueue_regions_from_sorted(w_, lc_, w_.kR, 0, (uint32_t) tiles, 0, s_));
+		if (rc) return rc;
+		sorted_v = w_.vR;
+	}
 	for (size_t r = 0; r < runs.size(); r++) {
 		rc = cuda_status(enqueue_stats_run(w_, runs_h_[r], (uint32_t) r,
-			w_.vR + base_h[r], runs[r].p.init_sheep + runs[r].p.init_wolves, 0, s_));
+			sorted_v + base_h[r], runs[r].p.init_sheep + runs[r].p.init_wolves, 0, s_));
 		if (rc) return rc;
 	}
 	giter_ = 0;
@@ -316,13 +342,34 @@ int World::sort_into(uint32_t n, uint32_t *dst_k, uint32_t *dst_v)
 	return PP_SUCCESS;
 }
 
+int World::place_sorted(uint32_t n, uint32_t first, uint32_t count,
+	uint32_t out_base)
+{
+	/* tile offsets of the n cell-sorted agents in A (count from
+	 * ctr->aux_n), the first move of the agents of tiles [first, first +
+	 * count) into the group buffer from out_base on, then the dense input
+	 * bases of the next act */
+	(void) n;
+	PP_CK(launch_offsets(w_.kA, &w_.ctr->aux_n, w_.log_tile, w_.n_tiles,
+		w_.tile_off, lc_.offs_blocks, s_));
+	PP_CK(enqueue_move_groups(w_, lc_, w_.kA, w_.vA, first, count, out_base, s_));
+	PP_CK(enqueue_fused_bases(w_, lc_, s_));
+	return PP_SUCCESS;
+}
+
+cudaError_t World::enqueue_one(const cudaEvent_t *marks)
+{
+	return w_.fused ? enqueue_iteration_fused(w_, lc_, s_, marks)
+		: enqueue_iteration(w_, lc_, s_, marks);
+}
+
 int World::build_graph()
 {
 	if (gexec_) { cudaGraphExecDestroy(gexec_); gexec_ = nullptr; }
 	if (graph_) { cudaGraphDestroy(graph_); graph_ = nullptr; }
 	PP_CK(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
 	for (uint32_t i = 0; i < graph_iters_; i++) {
-		cudaError_t e = enqueue_iteration(w_, lc_, s_);
+		cudaError_t e = enqueue_one();
 		if (e != cudaSuccess) {
 			cudaGraph_t g;
 			cudaStreamEndCapture(s_, &g);
@@ -351,7 +398,7 @@ int World::enqueue(uint32_t n)
 				k += graph_iters_;
 			}
 		}
-		for (; k < stretch; k++) PP_CK(enqueue_iteration(w_, lc_, s_));
+		for (; k < stretch; k++) PP_CK(enqueue_one());
 		giter_ += stretch;
 		done += stretch;
 		if (giter_ % REBASE == 0) PP_CK(enqueue_grass_rebase(w_, lc_, s_));
@@ -409,14 +456,22 @@ int World::get_state(uint32_t *cell, uint32_t *en, uint32_t n_max,
 {
 	PP_CK(cudaSetDevice(device_));
 	PP_CK(cudaStreamSynchronize(s_));
-	uint32_t n = 0;
+	if (w_.fused) {
+		int rc = get_state_fused(cell, en, n_max, n_out, r);
+		if (rc) return rc;
+		cell = nullptr;
+		en = nullptr;
+	}
+	uint32_t n = 0, m = 0;
+	if (!w_.fused) {
 	PP_CK(cudaMemcpy(&n, &w_.ctr->n_agents, 4, cudaMemcpyDeviceToHost));
 	if (n_out) *n_out = n;
-	uint32_t m = std::min(n, n_max);
+	m = std::min(n, n_max);
 	PP_CK(enqueue_compact(w_, lc_, w_.kA, w_.vA, s_));
 	PP_CK(cudaStreamSynchronize(s_));
 	if (cell && m) PP_CK(cudaMemcpy(cell, w_.kA, (size_t) m * 4, cudaMemcpyDeviceToHost));
 	if (en && m) PP_CK(cudaMemcpy(en, w_.vA, (size_t) m * 4, cudaMemcpyDeviceToHost));
+	}
 	if (grass) {
 		/* stored regrowth iterations -> countdowns of the current iteration */
 		const RunDev &run = runs_h_[r];
@@ -432,6 +487,79 @@ int World::get_state(uint32_t *cell, uint32_t *en, uint32_t n_max,
 		/* Report cells relative to the run's grid. */
 		uint32_t cb = runs_h_[r].cbase;
 		for (uint32_t i = 0; i < m; i++) cell[i] -= cb;
+	}
+	return PP_SUCCESS;
+}
+
+int World::get_state_fused(uint32_t *cell, uint32_t *en, uint32_t n_max,
+	uint32_t *n_out, uint32_t r)
+{
+	/* The state after the last act is the group buffer of the next parity:
+	 * every record of the run's tiles' inboxes (moved ones with their
+	 * direction, dead and parked ones in place), mapped back to the cell
+	 * before the move and the energy before it, in canonical order (cell,
+	 * rank in the cell's list). */
+	const RunDev &run = runs_h_[r];
+	const uint32_t p = (giter_ + 1) & 1;
+	const uint32_t T = 1u << w_.log_tile;
+	const size_t nt = run.n_tiles;
+	std::vector<uint32_t> inn(nt);
+	std::vector<uint2> ent(nt * IBX);
+	if (nt) {
+		const size_t ib = (size_t) p * w_.n_tiles + run.first_tile;
+		PP_CK(cudaMemcpy(inn.data(), w_.inbox_n + ib, nt * 4, cudaMemcpyDeviceToHost));
+		PP_CK(cudaMemcpy(ent.data(), w_.inbox + ib * IBX, nt * IBX * sizeof(uint2),
+			cudaMemcpyDeviceToHost));
+	}
+	/* the group buffer up to the end of the last listed group */
+	uint64_t top = 0;
+	for (size_t q = 0; q < nt; q++)
+		for (uint32_t i = 0; i < std::min(inn[q], IBX); i++) {
+			const uint2 e = ent[q * IBX + i];
+			top = std::max<uint64_t>(top, (uint64_t) e.x + (e.y & ~GROUP_GRAVE));
+		}
+	top = std::min<uint64_t>(top, 3ull * w_.cap);
+	std::vector<uint32_t> kg(top), vg(top);
+	if (top) {
+		PP_CK(cudaMemcpy(kg.data(), p ? w_.kG1 : w_.kG0, (size_t) top * 4, cudaMemcpyDeviceToHost));
+		PP_CK(cudaMemcpy(vg.data(), p ? w_.vG1 : w_.vG0, (size_t) top * 4, cudaMemcpyDeviceToHost));
+	}
+	d2h_ += (uint64_t) top * 8 + nt * (4 + IBX * sizeof(uint2)) + 4;
+	struct Rec { uint32_t cell, rank, val; };
+	std::vector<Rec> recs;
+	for (size_t q = 0; q < nt; q++) {
+		const uint32_t tile = run.first_tile + (uint32_t) q;
+		const uint32_t nin = std::min(inn[q], IBX);
+		for (uint32_t i = 0; i < nin; i++) {
+			const uint2 e = ent[q * IBX + i];
+			const uint32_t c = e.y & ~GROUP_GRAVE;
+			for (uint32_t a = e.x; a < e.x + c && a < top; a++) {
+				const uint32_t key = kg[a], val = vg[a];
+				const uint32_t code = (key >> REC_DIR_SHIFT) & 7u;
+				const uint32_t lr = (tile << w_.log_tile) + (key & (T - 1)) - run.cbase;
+				Rec rc;
+				rc.rank = key >> REC_RANK_SHIFT;
+				if (code <= 4) {
+					const uint32_t y = lr / run.gx, x = lr - y * run.gx;
+					rc.cell = (uint32_t) ((int64_t) lr + src_offset(code, x, y, run.gx, run.gy));
+					rc.val = val + 1;
+				} else {
+					rc.cell = lr;
+					rc.val = val;
+				}
+				recs.push_back(rc);
+			}
+		}
+	}
+	std::sort(recs.begin(), recs.end(), [](const Rec &a, const Rec &b) {
+		return a.cell != b.cell ? a.cell < b.cell : a.rank < b.rank;
+	});
+	const uint32_t n = (uint32_t) recs.size();
+	if (n_out) *n_out = n;
+	const uint32_t m = std::min(n, n_max);
+	for (uint32_t i = 0; i < m; i++) {
+		if (cell) cell[i] = recs[i].cell;
+		if (en) en[i] = recs[i].val;
 	}
 	return PP_SUCCESS;
 }
@@ -452,11 +580,32 @@ int World::profile(uint32_t n, pp_kernel_prof *prof, double *agent_steps)
 		if (runs_h_[r].active) live_cells += runs_h_[r].ncells;
 	double steps = 0;
 	int rc = PP_SUCCESS;
-	for (uint32_t it = 0; it < n && rc == PP_SUCCESS; it++) {
+	for (uint32_t it = 0; it < n && rc == PP_SUCCESS && w_.fused; it++) {
+		uint32_t n_before = 0, n_after = 0;
+		PP_CK(cudaMemcpyAsync(&n_before, &w_.ctr->n_agents, 4, cudaMemcpyDeviceToHost, s_));
+		PP_CK(cudaStreamSynchronize(s_));
+		rc = cuda_status(enqueue_one(ev.data()));
+		if (rc) break;
+		PP_CK(cudaMemcpyAsync(&n_after, &w_.ctr->n_agents, 4, cudaMemcpyDeviceToHost, s_));
+		PP_CK(cudaStreamSynchronize(s_));
+		giter_++;
+		float ms;
+		PP_CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+		prof[3].launches++; prof[3].total_ms += ms;
+		/* act+move: the tile's records in, survivors and newborns out as
+		 * moved records, the regrowth word of each occupied cell (at most
+		 * one read per agent) */
+		prof[3].bytes += 10.0 * n_before + 8.0 * n_after;
+		PP_CK(cudaEventElapsedTime(&ms, ev[1], ev[2]));
+		prof[4].launches++; prof[4].total_ms += ms;
+		prof[4].bytes += 48.0 * w_.n_tiles;
+		steps += n_before;
+	}
+	for (uint32_t it = 0; it < n && rc == PP_SUCCESS && !w_.fused; it++) {
 		uint32_t n_before = 0, n_live = 0, n_after = 0;
 		PP_CK(cudaMemcpyAsync(&n_before, &w_.ctr->n_agents, 4, cudaMemcpyDeviceToHost, s_));
 		PP_CK(cudaStreamSynchronize(s_));
-		rc = cuda_status(enqueue_iteration(w_, lc_, s_, ev.data()));
+		rc = cuda_status(enqueue_one(ev.data()));
 		if (rc) break;
 		PP_CK(cudaMemcpyAsync(&n_live, &w_.tile_off[w_.n_tiles], 4, cudaMemcpyDeviceToHost, s_));
 		PP_CK(cudaMemcpyAsync(&n_after, &w_.ctr->n_agents, 4, cudaMemcpyDeviceToHost, s_));
@@ -543,16 +692,29 @@ int World::admit(const RunSpec &spec, uint32_t *slot_out)
 	rc = cuda_status(enqueue_init_agents(run, w_.kB, w_.vB, 0,
 		spec.p.init_sheep, spec.p.init_wolves, s_));
 	if (rc) return rc;
-	/* The agents go to the admission area of the region buffer (after the
-	 * 2 * cap slots the act writes), as the regions of the run's tiles. */
-	const uint32_t adm = 2 * w_.cap + adm_used_;
-	rc = sort_into(n0, w_.kR + adm, w_.vR + adm);
-	if (rc) return rc;
-	rc = cuda_status(enqueue_regions_from_sorted(w_, lc_, w_.kR + adm, first, need, adm, s_));
-	if (rc) return rc;
-	adm_used_ += n0;
-	rc = cuda_status(enqueue_stats_run(w_, run, slot, w_.vR + adm, n0, row, s_));
-	if (rc) return rc;
+	if (w_.fused) {
+		/* sorted into A, moved into the group buffer the next act reads */
+		rc = sort_into(n0, w_.kA, w_.vA);
+		if (rc) return rc;
+		rc = place_sorted(n0, first, need, 2 * w_.cap + adm_used_);
+		if (rc) return rc;
+		adm_used_ += n0;
+		rc = cuda_status(enqueue_stats_run(w_, run, slot, w_.vA, n0, row, s_));
+		if (rc) return rc;
+		PP_CK(cudaStreamSynchronize(s_));
+	} else {
+		/* The agents go to the admission area of the region buffer (after
+		 * the 2 * cap slots the act writes), as the regions of the run's
+		 * tiles. */
+		const uint32_t adm = 2 * w_.cap + adm_used_;
+		rc = sort_into(n0, w_.kR + adm, w_.vR + adm);
+		if (rc) return rc;
+		rc = cuda_status(enqueue_regions_from_sorted(w_, lc_, w_.kR + adm, first, need, adm, s_));
+		if (rc) return rc;
+		adm_used_ += n0;
+		rc = cuda_status(enqueue_stats_run(w_, run, slot, w_.vR + adm, n0, row, s_));
+		if (rc) return rc;
+	}
 	h2d_ += sizeof(RunDev) + need * 2;
 	d2h_ += 4;
 	*slot_out = slot;
@@ -628,7 +790,7 @@ extern "C" void pp_opts_default(pp_opts *o)
 	o->tile_cells = 0;
 	o->sort_digit_bits = 0;
 	o->use_graph = 1;
-	o->unfused = 0;
+	o->sort_pipeline = 0;
 }
 
 extern "C" int pp_sim_create(const PPParameters *params, uint64_t seed,
@@ -656,6 +818,7 @@ extern "C" int pp_sim_create(const PPParameters *params, uint64_t seed,
 	cfg.tile_cells = o.tile_cells;
 	cfg.digit_bits = o.sort_digit_bits;
 	cfg.graph_iters = o.use_graph ? 32 : 0;
+	cfg.fused = o.sort_pipeline == 0;
 	std::vector<RunSpec> runs(1);
 	runs[0].p = p;
 	runs[0].seed = seed;

@@ -30,6 +30,7 @@ struct WorldConfig {
 	uint32_t extra_tiles = 0;      /* free tile space for later admissions */
 	uint32_t act_cap = 0;          /* 0 = choose */
 	uint32_t max_cells_hint = 0;   /* largest run (cells), for serving worlds */
+	bool fused = true;             /* fused act+move iteration (else the sort pipeline) */
 };
 
 class World {
@@ -67,12 +68,14 @@ public:
 	size_t bytes() const { return bytes_; }
 	uint32_t ring_rows() const { return w_.ring_rows; }
 	uint32_t tile_cells() const { return 1u << w_.log_tile; }
+	bool fused() const { return w_.fused != 0; }
 	int get_state(uint32_t *cell, uint32_t *en, uint32_t n_max,
 		uint32_t *n_out, uint16_t *grass, uint32_t r);
 
 	/* Run n iterations without graphs, timing every kernel with CUDA
 	 * events on the world's stream; fills prof[0..4] (move, radix pass,
-	 * offsets, act, finish) with algorithmic bytes. */
+	 * offsets, act, finish) with algorithmic bytes (the fused pipeline
+	 * launches only act and finish). */
 	int profile(uint32_t n, pp_kernel_prof *prof, double *agent_steps);
 
 private:
@@ -80,6 +83,11 @@ private:
 	int sort_into(uint32_t n, uint32_t *dst_k, uint32_t *dst_v);
 	int build_graph();
 	int init_run_device(uint32_t r, uint32_t base, const RunSpec &spec);
+	cudaError_t enqueue_one(const cudaEvent_t *marks = nullptr);
+	int get_state_fused(uint32_t *cell, uint32_t *en, uint32_t n_max,
+		uint32_t *n_out, uint32_t r);
+	int place_sorted(uint32_t n, uint32_t first, uint32_t count,
+		uint32_t out_base);
 	void free_all();
 
 	int device_ = 0;

@@ -9,6 +9,9 @@ from common import params, rows_array, first_diff
 
 pytestmark = pytest.mark.gpu
 
+# both iteration pipelines: fused act+move (default) and the sort pipeline
+PIPES = pytest.mark.parametrize("sort_pipeline", [False, True], ids=["fused", "sort"])
+
 
 def _check_run(p, seed, iters, **kw):
     got = rows_array(pp.run(p, seed, iters, **kw))
@@ -21,18 +24,27 @@ def _check_run(p, seed, iters, **kw):
 @pytest.mark.parametrize("side,version,seed,iters", [
     (25, 1, 0, 400), (25, 2, 1, 300), (50, 1, 2, 500), (50, 2, 3, 300),
     (100, 1, 0, 1000), (64, 2, 9, 200), (33, 1, 17, 300)])
-def test_stats_bit_exact(side, version, seed, iters):
-    _check_run(params(side, version), seed, iters)
+@PIPES
+def test_stats_bit_exact(side, version, seed, iters, sort_pipeline):
+    _check_run(params(side, version), seed, iters, sort_pipeline=sort_pipeline)
 
 
-@pytest.mark.parametrize("tile", [1024, 2048, 4096])
-def test_tile_sizes_agree(tile):
-    _check_run(params(70, 2), 5, 150, tile_cells=tile)
+@PIPES
+@pytest.mark.parametrize("tile", [1024, 2048, 4096, 8192])
+def test_tile_sizes_agree(tile, sort_pipeline):
+    _check_run(params(70, 2), 5, 150, tile_cells=tile, sort_pipeline=sort_pipeline)
 
 
 @pytest.mark.parametrize("digit_bits", [5, 6, 8])
 def test_digit_widths_agree(digit_bits):
-    _check_run(params(60, 1), 4, 150, digit_bits=digit_bits)
+    _check_run(params(60, 1), 4, 150, digit_bits=digit_bits, sort_pipeline=True)
+
+
+def test_wide_grid_many_tiles():
+    # rows longer than a tile: moves across tile edges in x and y, with the
+    # per-row wrap landing in far tiles
+    _check_run(params(0, 1, gx=9000, gy=7, sheep=2500, wolves=1200), 13, 120,
+               tile_cells=1024)
 
 
 def test_without_graph():
@@ -41,8 +53,10 @@ def test_without_graph():
 
 @pytest.mark.parametrize("gx,gy,s,w", [(1, 1, 5, 3), (1, 50, 20, 10), (50, 1, 20, 10),
                                        (7, 13, 40, 20), (300, 2, 30, 30)])
-def test_degenerate_grids(gx, gy, s, w):
-    _check_run(params(0, 1, gx=gx, gy=gy, sheep=s, wolves=w), 3, 120)
+@PIPES
+def test_degenerate_grids(gx, gy, s, w, sort_pipeline):
+    _check_run(params(0, 1, gx=gx, gy=gy, sheep=s, wolves=w), 3, 120,
+               sort_pipeline=sort_pipeline)
 
 
 @pytest.mark.parametrize("s,w", [(0, 0), (50, 0), (0, 50)])
@@ -50,18 +64,20 @@ def test_single_species_and_empty(s, w):
     _check_run(params(30, 1, sheep=s, wolves=w), 8, 150)
 
 
-def test_crowded_cells():
+@PIPES
+def test_crowded_cells(sort_pipeline):
     # many agents per cell: exercises long in-cell orderings and the
     # shared-memory overflow path of the act kernel
     _check_run(params(0, 2, gx=20, gy=20, sheep=3000, wolves=1500), 12, 60,
-               max_agents=400_000)
+               max_agents=400_000, sort_pipeline=sort_pipeline)
 
 
-def test_state_bit_exact_after_steps():
+@PIPES
+def test_state_bit_exact_after_steps(sort_pipeline):
     p = params(40, 2)
     seed = 21
     o = orc.State(p, seed, capacity=1 << 20)
-    with pp.Simulation(p, seed, max_agents=1 << 20) as sim:
+    with pp.Simulation(p, seed, max_agents=1 << 20, sort_pipeline=sort_pipeline) as sim:
         cell, en, grass = sim.state()
         ocell, oen = o.agents()
         assert np.array_equal(cell, ocell) and np.array_equal(en, oen)
@@ -86,10 +102,11 @@ def test_chunked_steps_equal_single_call():
     assert np.array_equal(a, rows_array(rows))
 
 
-def test_pool_overflow_reports_error():
+@PIPES
+def test_pool_overflow_reports_error(sort_pipeline):
     p = params(50, 2)
     with pytest.raises(pp.PPError) as ei:
-        pp.run(p, 1, 200, max_agents=1500)
+        pp.run(p, 1, 200, max_agents=1500, sort_pipeline=sort_pipeline)
     assert ei.value.code == pp.PP_OUT_OF_RESOURCES
 
 
