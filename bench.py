@@ -10,13 +10,24 @@ A "step" is one simulation iteration over the whole grid.
 
 ours:       W untimed iterations, then K iterations timed with CUDA events
             on the simulation's stream (graph replay; state resident in
-            HBM; the working set, ~1.6 GB, exceeds the 129 MB L2). value =
+            HBM; the working set, ~2 GB, exceeds the 129 MB L2). value =
             agent-steps / s over all ranks. `e2e` is a whole job through the
             C ABI from the host: pp_sim_create (parameters and run tables
             copied in, state initialised on the GPU), the iterations with
             every stats row copied back to a host buffer, pp_sim_destroy.
             `roofline` comes from per-kernel CUDA events (pp_sim_profile)
-            over a few further iterations.
+            over a few further iterations; its algorithmic bytes are the
+            per-iteration figure of the reference-shaped step,
+            12 C + (16 + 16 P + 16) N bytes (C cells, N agents at the
+            iteration's start, P = 4 sort passes at this grid size; the
+            8 bytes per birth are left out), attributed to the fused
+            act+move kernel, which does the whole iteration but the stats.
+            `batched` runs the 64-run mix (32 x 200^2 v1, 16 x 800^2 v2,
+            8 x 1600^2 v1, 8 x 3200^2 v2, seeds 100..163, --batch-iters
+            iterations each) once through pp_batch_run (one world, every
+            launch shared) and once run by run through pp_sim_* (one run per
+            launch sequence), both end to end with host stats buffers, and
+            checks that every run's stats agree bit for bit.
 reference:  the CPU restatement of the reference's CPU algorithm
             (oracle/pp_cpu_port.c: row-banded pp_cpu semantics, OpenMP over
             all host cores; the reference itself cannot be built here) on
@@ -24,6 +35,15 @@ reference:  the CPU restatement of the reference's CPU algorithm
 With N > 1 (torchrun), every rank runs an independent replica (the runs
 do not exchange data); the timed region is bracketed by barriers and the
 slowest rank's time is used.
+
+  python bench.py --workload served
+
+prints one line for the served workload instead: a Poisson stream (20
+requests/s) of 1000 runs, side uniform in {100, ..., 3200}, parameter set
+v1 or v2 (p = 0.5), iterations uniform in [500, 4000], sequential seeds,
+admitted into one continuously batched world under a 150 GB budget; p50 /
+p99 completion latency (arrival to last stats row on the host) and
+aggregate agent-steps/s.
 """
 import argparse
 import json
@@ -43,6 +63,37 @@ WORKLOAD = dict(init_sheep=6553600, sheep_gain_from_food=4,
                 grass_restart=10, grid_x=12800, grid_y=12800, iters=4000)
 SEED = 2
 WORKLOAD_NAME = "pphpc-12800x12800-v1"
+
+# Parameter sets v1 and v2 (the reference's configs/config*v1.txt and
+# *v2.txt); agents scale with the grid area (400 sheep and 200 wolves per
+# 100 x 100 cells for both).
+V1 = dict(sheep_gain_from_food=4, sheep_reproduce_threshold=2,
+          sheep_reproduce_prob=4, wolves_gain_from_food=20,
+          wolves_reproduce_threshold=2, wolves_reproduce_prob=5,
+          grass_restart=10)
+V2 = dict(sheep_gain_from_food=30, sheep_reproduce_threshold=2,
+          sheep_reproduce_prob=10, wolves_gain_from_food=10,
+          wolves_reproduce_threshold=2, wolves_reproduce_prob=5,
+          grass_restart=15)
+MIX = [(200, 1, 32), (800, 2, 16), (1600, 1, 8), (3200, 2, 8)]
+POOL_FACTOR = 40     # v2 populations peak near 36x their initial agents
+
+
+def scaled_params(pp, side, version, iters):
+    area = side * side
+    return pp.make_params(init_sheep=area * 4 // 100, init_wolves=area * 2 // 100,
+                          grid_x=side, grid_y=side, iters=iters,
+                          **(V1 if version == 1 else V2))
+
+
+def spec_bytes_per_iter(cells, n_agents):
+    """Per-iteration bytes of the reference-shaped step: 12 bytes per cell
+    (grass read + write, cell offsets written and read) and 16 + 16 P + 16
+    bytes per agent (move, P sort passes, act), P = ceil((ceil(log2 C) +
+    1) / 8) 8-bit digit passes; births (8 bytes each) are not counted."""
+    import math
+    P = math.ceil((math.ceil(math.log2(cells)) + 1) / 8)
+    return 12.0 * cells + (32.0 + 16.0 * P) * n_agents, P
 
 
 def dist_env():
@@ -191,20 +242,25 @@ def run_ours(args, dist):
     prof_iters = min(max(K // 2, 4), 16)
     kernels, prof_steps = sim.profile(prof_iters)
     sim.close()
+    kernels = [k for k in kernels if k[1]]
     dom = max(kernels, key=lambda k: k[2])
     name, launches, tot_ms, byts = dom
     peak, peak_kind = measured_peaks()
-    achieved = (byts / launches) / ((tot_ms / launches) / 1e3) / 1e9
+    cells = p.grid_x * p.grid_y
+    n_avg = prof_steps / prof_iters
+    spec_b, P = spec_bytes_per_iter(cells, n_avg)
+    achieved = spec_b / ((tot_ms / launches) / 1e3) / 1e9
     traffic = None
     tr = ncu_traffic().get(name)
     if tr:
         unit = tr.get("per")
         if unit == "agent":
-            traffic = tr["bytes_per_unit"] * (prof_steps / prof_iters)
+            traffic = tr["bytes_per_unit"] * n_avg
         elif unit == "launch":
             traffic = tr["bytes_per_launch"]
     step_bytes = sum(k[3] for k in kernels) / prof_iters
     step_ms = sum(k[2] for k in kernels) / prof_iters
+    timed_spec_bytes = sum(spec_bytes_per_iter(cells, r.sheep + r.wolves)[0] for r in rows)
 
     # -- end to end through the C ABI with host buffers --
     dist.barrier()
@@ -237,22 +293,131 @@ def run_ours(args, dist):
         "gpu_launches": None,
         "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "algorithmic_bytes_per_launch": byts / launches,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": spec_b,
+                     "algorithmic_bytes": "12 C + (32 + 16 P) N, P = %d, N = %.0f" % (P, n_avg),
                      "avg_launch_ms": tot_ms / launches},
-        "step_roofline": {"algorithmic_bytes_per_step": step_bytes,
-                          "kernel_ms_per_step": step_ms,
-                          "achieved_gbs": step_bytes / (step_ms / 1e3) / 1e9,
-                          "frac": step_bytes / (step_ms / 1e3) / 1e9 / peak},
+        "timed_roofline": {"algorithmic_bytes": timed_spec_bytes,
+                           "achieved_gbs": timed_spec_bytes / (ms_max / 1e3) / 1e9,
+                           "frac": timed_spec_bytes / (ms_max / 1e3) / 1e9 / peak,
+                           "note": "same per-iteration figure over the K timed "
+                                   "iterations and their whole device time"},
+        "kernel_bytes": {"moved_bytes_per_step": step_bytes,
+                         "kernel_ms_per_step": step_ms,
+                         "achieved_gbs": step_bytes / (step_ms / 1e3) / 1e9,
+                         "note": "bytes the kernels must move in this design "
+                                 "(records in and out, occupied cells' grass)"},
         "kernels": [{"name": k[0], "launches": k[1], "ms": k[2], "bytes": k[3],
                      "gbs": (k[3] / (k[2] / 1e3) / 1e9) if k[2] > 0 else None}
                     for k in kernels],
         "clocks": clk,
     }
-    passes = next((k[1] for k in kernels if k[0] == "radix_pass"), 0) // prof_iters
-    out["gpu_launches"] = K * (3 + passes)
+    launches_per_iter = sum(k[1] for k in kernels) // prof_iters
+    out["gpu_launches"] = K * launches_per_iter
+    if args.batch_iters > 0:
+        out["batched"] = batched_vs_plain(args, dist)
     if dist.rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args)
     return out
+
+
+def batched_vs_plain(args, dist):
+    """The 64-run mix through pp_batch_run (one world) and run by run
+    through pp_sim_* (one world per run), both end to end with host stats
+    buffers; aggregate agent-steps/s of each, and whether every run's stats
+    agree bit for bit."""
+    import pphpc_gb300 as pp
+    iters = args.batch_iters
+    runs = []
+    seed = 100
+    for side, version, n in MIX:
+        for _ in range(n):
+            runs.append((scaled_params(pp, side, version, iters), seed))
+            seed += 1
+    dev = dist.local
+    dist.barrier()
+    t0 = time.perf_counter()
+    out_b = pp.batch_run(runs, pool_factor=POOL_FACTOR, device=dev)
+    t1 = time.perf_counter()
+    out_p = []
+    for p, sd in runs:
+        n0 = p.init_sheep + p.init_wolves
+        out_p.append(pp.run(p, sd, device=dev, max_agents=POOL_FACTOR * n0))
+    t2 = time.perf_counter()
+    steps = 0
+    exact = True
+    for rb, rp in zip(out_b, out_p):
+        steps += sum(r.sheep + r.wolves for r in rb[:-1])
+        exact &= [r.as_tuple() for r in rb] == [r.as_tuple() for r in rp]
+    tb = dist.max(t1 - t0)
+    tp = dist.max(t2 - t1)
+    steps_all = dist.sum(float(steps))
+    return {"runs": len(runs), "iterations": iters,
+            "mix": "32x200^2 v1, 16x800^2 v2, 8x1600^2 v1, 8x3200^2 v2, seeds 100..163",
+            "agent_steps": steps_all,
+            "batched_s": tb, "plain_s": tp,
+            "batched_agent_steps_per_s": steps_all / tb,
+            "plain_agent_steps_per_s": steps_all / tp,
+            "speedup": tp / tb, "bit_exact_batched_vs_plain": bool(exact),
+            "timing": "wall clock, end to end through the C ABI (create, "
+                      "iterations, stats rows to host, destroy)"}
+
+
+def run_served(args, dist):
+    """The served workload: Poisson arrivals into pp_serve_*; returns p50 /
+    p99 completion latency and aggregate agent-steps/s."""
+    import random
+    import pphpc_gb300 as pp
+    if dist.rank != 0:
+        return None
+    rng = random.Random(20)
+    n_req = args.served_requests
+    t_arr = 0.0
+    reqs = []
+    for i in range(n_req):
+        t_arr += rng.expovariate(20.0)
+        side = rng.choice([100, 200, 400, 800, 1600, 3200])
+        version = 1 if rng.random() < 0.5 else 2
+        iters = rng.randint(500, 4000)
+        reqs.append((t_arr, scaled_params(pp, side, version, iters), 1000 + i))
+    srv = pp.Server(mem_budget_bytes=150 << 30, max_runs=1024, pool_factor=POOL_FACTOR,
+                    stats_chunk=64, device=dist.local)
+    pending = {}
+    lat = []
+    steps = 0
+    nxt = 0
+    t0 = time.perf_counter()
+    while len(lat) < n_req:
+        now = time.perf_counter() - t0
+        while nxt < n_req and reqs[nxt][0] <= now:
+            a, p, sd = reqs[nxt]
+            pending[srv.submit(p, sd)] = a
+            nxt += 1
+        if not pending:
+            time.sleep(max(0.0, reqs[nxt][0] - now))
+            continue
+        srv.poll(16)
+        now = time.perf_counter() - t0
+        for rid in list(pending):
+            ev = srv.status(rid)
+            if ev.done:
+                if ev.status != 0:
+                    raise RuntimeError("request %d failed (%d)" % (rid, ev.status))
+                rows = srv.read(rid)
+                steps += sum(r.sheep + r.wolves for r in rows[:-1])
+                lat.append(now - pending.pop(rid))
+                srv.release(rid)
+    wall = time.perf_counter() - t0
+    srv.close()
+    lat.sort()
+    q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))]
+    return {"metric": "completion latency", "workload": "served",
+            "requests": n_req, "arrival_rate_per_s": 20.0,
+            "p50_s": q(0.50), "p99_s": q(0.99), "mean_s": sum(lat) / len(lat),
+            "agent_steps": steps, "wall_s": wall,
+            "agent_steps_per_s": steps / wall, "unit": "s",
+            "higher_is_better": False, "n_gpus": 1,
+            "config": {"workload": "served: Poisson 20/s, side in {100..3200}, "
+                                   "v1/v2 p=0.5, iters U[500,4000], 150 GB budget"}}
 
 
 def cpu_baseline(args):
@@ -288,6 +453,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-iters", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-iters", type=int, default=4000,
+                    help="iterations per run of the batched-vs-plain mix (0 = skip)")
+    ap.add_argument("--workload", choices=["plain", "served"], default="plain")
+    ap.add_argument("--served-requests", type=int, default=1000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -295,6 +464,8 @@ def main():
     try:
         if args.impl == "reference":
             out = run_reference(args, dist)
+        elif args.workload == "served":
+            out = run_served(args, dist)
         else:
             out = run_ours(args, dist)
         if dist.rank == 0 and out is not None:

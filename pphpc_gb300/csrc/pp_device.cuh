@@ -167,7 +167,7 @@ struct WorldCounters {
 	uint32_t aux_n;          /* element count of a standalone sort        */
 	uint32_t fin_ticket;     /* finish chunk tickets                      */
 	uint32_t n_all;          /* fused finish: records counted so far       */
-	uint32_t pad;
+	uint32_t tile_hi;        /* tiles [0, tile_hi) hold runs (fused act)   */
 };
 
 /* ---- memory-ordering helpers ---- */

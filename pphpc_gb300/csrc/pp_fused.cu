@@ -22,6 +22,8 @@
  * sums each tile's posted group sizes into the dense input bases of the
  * next act, so no act allocates with an atomic on a shared counter.
  */
+#include <algorithm>
+
 #include "pp_act.cuh"
 
 namespace pp {
@@ -148,11 +150,10 @@ __device__ __forceinline__ uint32_t step_excl_scan(uint32_t v, uint32_t *total)
  * one warp allocates the tile's groups and posts them to the destination
  * tiles' inboxes; E2 records into the groups; per-tile stats. */
 template <int CPT, bool ACT>
-__global__ void __launch_bounds__(NT, 8) k_step(WorldDev w,
+__device__ __forceinline__ void step_tile(const WorldDev &w,
 	const uint32_t *__restrict__ kS, const uint32_t *__restrict__ vS,
-	uint32_t tile0, uint32_t out_base)
+	uint32_t tile, uint32_t out_base, uint32_t *sm)
 {
-	extern __shared__ __align__(16) uint32_t sm[];
 	uint32_t *sk = sm, *sv = sm + w.act_cap, *sp = sv + w.act_cap,
 		*sd = sp + w.act_cap, *sperm = sd + w.act_cap;
 	uint32_t *scnt = sperm + w.act_cap;                 /* CPT * NT */
@@ -162,7 +163,6 @@ __global__ void __launch_bounds__(NT, 8) k_step(WorldDev w,
 	__shared__ uint32_t s_xbase, s_fail;
 
 	const uint32_t tid = threadIdx.x, lane = tid & 31;
-	const uint32_t tile = tile0 + blockIdx.x;
 	const uint32_t c0 = tile << w.log_tile;
 	/* loads that depend on nothing, issued first: the tile's grass (async
 	 * copy into shared memory), both parities' inboxes (every warp reads
@@ -233,11 +233,12 @@ __global__ void __launch_bounds__(NT, 8) k_step(WorldDev w,
 	}
 	const bool in_smem = m <= w.act_cap;
 	if (!in_smem) {
-		/* crowded tile: its arrays go to global scratch (3 m slots: the
-		 * permutation, then the output map and the move directions) */
+		/* crowded tile: its arrays go to global scratch (m slots of each
+		 * array; 3 m of the permutation array, which then holds the output
+		 * map and the move directions) */
 		if (tid == 0) {
-			const uint32_t b = atomicAdd(&w.ctr->xtop, 3 * m);
-			s_fail = (uint64_t) b + 3ull * m > w.cap;
+			const uint32_t b = atomicAdd(&w.ctr->xtop, m);
+			s_fail = (uint64_t) b + m > w.cap;
 			if (s_fail) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
 			s_xbase = b;
 		}
@@ -254,7 +255,7 @@ __global__ void __launch_bounds__(NT, 8) k_step(WorldDev w,
 	} else {
 		const uint32_t xb = s_xbase;
 		UK = w.scratch_prio + xb; UV = w.scratch_kid + xb;
-		PERM = w.scratch_perm + xb;
+		PERM = w.scratch_perm + 3ull * xb;
 		LK = w.scratch_key + xb; LV = w.scratch_val + xb;
 	}
 	uint32_t *LP = UK, *LD = UV;      /* priorities / dice, then offsets / kids */
@@ -599,6 +600,28 @@ __global__ void __launch_bounds__(NT, 8) k_step(WorldDev w,
 	}
 }
 
+/* The fused act: one CTA per tile below the world's high-water mark (the
+ * host sizes the grid from it and moves it when runs are admitted or
+ * retired), so a serving world's free tile space costs nothing. */
+template <int CPT>
+__global__ void __launch_bounds__(NT, 8) k_step_act(WorldDev w)
+{
+	extern __shared__ __align__(16) uint32_t sm[];
+	if (blockIdx.x >= min(w.ctr->tile_hi, w.n_tiles)) return;
+	step_tile<CPT, true>(w, nullptr, nullptr, blockIdx.x, 0, sm);
+}
+
+/* The first move of a freshly initialised run: one CTA per tile of
+ * [tile0, tile0 + gridDim.x). */
+template <int CPT>
+__global__ void __launch_bounds__(NT, 8) k_step_first(WorldDev w,
+	const uint32_t *__restrict__ kS, const uint32_t *__restrict__ vS,
+	uint32_t tile0, uint32_t out_base)
+{
+	extern __shared__ __align__(16) uint32_t sm[];
+	step_tile<CPT, false>(w, kS, vS, tile0 + blockIdx.x, out_base, sm);
+}
+
 template <bool ACT>
 cudaError_t launch_step(const WorldDev &w, const LaunchCfg &lc,
 	const uint32_t *k, const uint32_t *v, uint32_t first, uint32_t count,
@@ -607,12 +630,21 @@ cudaError_t launch_step(const WorldDev &w, const LaunchCfg &lc,
 	const uint32_t T = 1u << w.log_tile;
 	const size_t smem = (size_t) w.act_cap * 5 * sizeof(uint32_t)
 		+ (size_t) T * (sizeof(uint32_t) + sizeof(uint16_t));
-	(void) lc;
-	switch (T / NT) {
-	case 8: k_step<8, ACT><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
-	case 16: k_step<16, ACT><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
-	case 32: k_step<32, ACT><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
-	default: k_step<64, ACT><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
+	if (ACT) {
+		const uint32_t grid = (uint32_t) std::max(1, lc.act_tiles);
+		switch (T / NT) {
+		case 8: k_step_act<8><<<grid, NT, smem, s>>>(w); break;
+		case 16: k_step_act<16><<<grid, NT, smem, s>>>(w); break;
+		case 32: k_step_act<32><<<grid, NT, smem, s>>>(w); break;
+		default: k_step_act<64><<<grid, NT, smem, s>>>(w); break;
+		}
+	} else {
+		switch (T / NT) {
+		case 8: k_step_first<8><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
+		case 16: k_step_first<16><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
+		case 32: k_step_first<32><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
+		default: k_step_first<64><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
+		}
 	}
 	return cudaGetLastError();
 }
@@ -620,11 +652,23 @@ cudaError_t launch_step(const WorldDev &w, const LaunchCfg &lc,
 template <int CPT>
 cudaError_t set_step_limit(size_t bytes)
 {
-	cudaError_t e = cudaFuncSetAttribute(k_step<CPT, true>,
+	cudaError_t e = cudaFuncSetAttribute(k_step_act<CPT>,
 		cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
 	if (e != cudaSuccess) return e;
-	return cudaFuncSetAttribute(k_step<CPT, false>,
+	return cudaFuncSetAttribute(k_step_first<CPT>,
 		cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+}
+
+template <int CPT>
+int step_occupancy(size_t smem)
+{
+	int n = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_act<CPT>, NT, smem)
+		!= cudaSuccess) {
+		cudaGetLastError();
+		return 1;
+	}
+	return n;
 }
 
 } /* namespace */
@@ -649,6 +693,16 @@ cudaError_t enqueue_move_groups(const WorldDev &w, const LaunchCfg &lc,
 {
 	if (count == 0) return cudaSuccess;
 	return launch_step<false>(w, lc, k, v, first, count, out_base, s);
+}
+
+int occupancy_step(uint32_t tile_cells, size_t smem)
+{
+	switch (tile_cells / NT) {
+	case 8: return step_occupancy<8>(smem);
+	case 16: return step_occupancy<16>(smem);
+	case 32: return step_occupancy<32>(smem);
+	default: return step_occupancy<64>(smem);
+	}
 }
 
 cudaError_t set_step_smem_limits(size_t bytes)

@@ -472,9 +472,11 @@ __global__ void __launch_bounds__(256) k_finish(WorldDev w)
 	const uint32_t g = w.ctr->giter + 1;
 	const uint32_t row = g % w.ring_rows;
 	const uint32_t epoch = w.ctr->seq * 8u + 7u;
-	const uint32_t per = (w.n_tiles + gridDim.x - 1) / gridDim.x;
-	const uint32_t t0 = min(chunk * per, w.n_tiles);
-	const uint32_t t1 = min(t0 + per, w.n_tiles);
+	/* fused pipeline: only tiles below the high-water mark hold runs */
+	const uint32_t nt = FUSED ? min(w.ctr->tile_hi, w.n_tiles) : w.n_tiles;
+	const uint32_t per = (nt + gridDim.x - 1) / gridDim.x;
+	const uint32_t t0 = min(chunk * per, nt);
+	const uint32_t t1 = min(t0 + per, nt);
 	if (FULL) {
 		const uint32_t r0 = t0 < t1 ? w.tile_run[t0] : 0;
 		bool same = true;

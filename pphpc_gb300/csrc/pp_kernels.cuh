@@ -53,6 +53,7 @@ struct WorldDev {
 struct LaunchCfg {
 	int sms;
 	int move_blocks, sort_blocks, offs_blocks, finish_blocks;
+	int act_tiles;            /* fused act grid: tiles below the high-water mark */
 	int cpt;                  /* cells per act thread (4, 8, 16 or 32)      */
 };
 
@@ -84,6 +85,7 @@ cudaError_t enqueue_fused_bases(const WorldDev &w, const LaunchCfg &lc,
 	cudaStream_t s);
 
 cudaError_t set_step_smem_limits(size_t bytes);
+int occupancy_step(uint32_t tile_cells, size_t smem);
 
 /* Initialisation of a run: grass of its tiles; its initial agents in
  * creation order into k/v[base ..) (sorted by cell afterwards); the stats

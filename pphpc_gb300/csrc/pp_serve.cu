@@ -81,9 +81,9 @@ extern "C" int pp_serve_create(const pp_serve_opts *opts, pp_server **out)
 	if (!srv) return PP_OUT_OF_RESOURCES;
 	srv->opts = o;
 	/* Budget split: a tile costs 2 B per cell (grass) plus ~610 B of
-	 * per-tile tables (inboxes, offsets, partial stats), an agent slot 93 B
+	 * per-tile tables (inboxes, offsets, partial stats), an agent slot 101 B
 	 * (three key/value arrays for sorting a new run's agents, two group
-	 * buffers of three slots per agent, five scratch words for crowded
+	 * buffers of three slots per agent, seven scratch words for crowded
 	 * tiles, sort look-back). Cells are bounded by the 2^31 key space. */
 	const uint32_t T = 2048;
 	const uint64_t tile_bytes = T * 2ull + 610;
@@ -94,7 +94,7 @@ extern "C" int pp_serve_create(const pp_serve_opts *opts, pp_server **out)
 	if (tiles > max_tiles) tiles = max_tiles;
 	if (tiles < 1) tiles = 1;
 	uint64_t rest = budget > tiles * tile_bytes ? budget - tiles * tile_bytes : 0;
-	uint64_t cap = rest / 93;
+	uint64_t cap = rest / 101;
 	if (cap > 0x7fffffffull) cap = 0x7fffffffull;
 	if (cap < 4096) cap = 4096;
 	WorldConfig cfg;

@@ -47,11 +47,13 @@ void choose_geometry(uint32_t total_cells, uint32_t cap, WorldConfig &cfg)
 {
 	if (cfg.tile_cells == 0) {
 		/* Dense worlds (many agents per cell) take smaller tiles so a
-		 * tile's agents fit in shared memory. */
+		 * tile's agents fit in shared memory; the fused act is latency
+		 * bound per tile and prefers more, smaller tiles in flight (eight
+		 * 128-thread CTAs per SM) than the sort pipeline's act. */
 		double dens = total_cells ? (double) cap / total_cells : 1.0;
-		cfg.tile_cells = dens > 1.0 ? 1024 : 4096;
+		if (dens > 1.0) cfg.tile_cells = 1024;
+		else cfg.tile_cells = cfg.fused ? 2048 : 4096;
 	}
-	(void) cap;
 }
 
 World::~World() { free_all(); }
@@ -204,7 +206,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	}
 	PP_AL(w_.scratch_key, cap * 4); PP_AL(w_.scratch_val, cap * 4);
 	PP_AL(w_.scratch_prio, cap * 4); PP_AL(w_.scratch_kid, cap * 4);
-	PP_AL(w_.scratch_perm, cap * 4);
+	PP_AL(w_.scratch_perm, (w_.fused ? 3 : 1) * cap * 4);
 	PP_AL(w_.rstart, (size_t) tiles * 4);
 	PP_AL(w_.rcnt, (size_t) tiles * 4);
 	PP_AL(w_.dbase, ((size_t) tiles + 1) * 4);
@@ -256,6 +258,8 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	PP_CK(cudaMemcpyAsync(w_.runs, runs_h_.data(), nruns_cap * sizeof(RunDev), cudaMemcpyHostToDevice, s_));
 	PP_CK(cudaMemcpyAsync(w_.tile_run, tile_run_h_.data(), tiles * 2, cudaMemcpyHostToDevice, s_));
 	WorldCounters c{};
+	tile_hi_ = used_tiles_;
+	c.tile_hi = tile_hi_;
 	PP_CK(cudaMemcpyAsync(w_.ctr, &c, sizeof(c), cudaMemcpyHostToDevice, s_));
 	h2d_ += nruns_cap * sizeof(RunDev) + tiles * 2 + sizeof(c);
 
@@ -271,6 +275,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	lc_.move_blocks = (int) std::max<uint64_t>(1, std::min<uint64_t>((tiles + 7) / 8, (uint64_t) sms * 8));
 	lc_.offs_blocks = sms * 8;
 	lc_.finish_blocks = (int) std::min<uint64_t>(tiles, (uint64_t) sms * 2);
+	lc_.act_tiles = (int) std::max<uint32_t>(tile_hi_, 1);
 
 	/* Initial state: grass, then every run's agents in creation order into
 	 * B at the run's base, sorted by cell into the region buffer (runs
@@ -639,6 +644,24 @@ int World::profile(uint32_t n, pp_kernel_prof *prof, double *agent_steps)
 	return sync_check();
 }
 
+int World::update_tile_hi()
+{
+	/* tiles of active runs and of retired runs still in quarantine */
+	uint32_t hi = 0;
+	for (uint32_t r = 0; r < null_slot_; r++)
+		if (runs_h_[r].active) hi = std::max(hi, runs_h_[r].first_tile + runs_h_[r].n_tiles);
+	for (auto &pt : pending_tiles_) hi = std::max(hi, pt.first.first + pt.first.second);
+	if (hi == tile_hi_) return PP_SUCCESS;
+	tile_hi_ = hi;
+	lc_.act_tiles = (int) std::max<uint32_t>(tile_hi_, 1);
+	PP_CK(cudaMemcpyAsync(&w_.ctr->tile_hi, &tile_hi_, 4, cudaMemcpyHostToDevice, s_));
+	PP_CK(cudaStreamSynchronize(s_));
+	h2d_ += 4;
+	/* the captured iterations carry the old grid */
+	if (gexec_ && graph_iters_) return build_graph();
+	return PP_SUCCESS;
+}
+
 bool World::fits(const RunSpec &spec) const
 {
 	uint32_t need = ceil_div((uint64_t) spec.p.grid_x * spec.p.grid_y,
@@ -683,6 +706,8 @@ int World::admit(const RunSpec &spec, uint32_t *slot_out)
 	for (uint32_t t = 0; t < need; t++) tile_run_h_[first + t] = (uint16_t) slot;
 	PP_CK(cudaMemcpyAsync(&w_.runs[slot], &run, sizeof(RunDev), cudaMemcpyHostToDevice, s_));
 	PP_CK(cudaMemcpyAsync(&w_.tile_run[first], &tile_run_h_[first], need * 2, cudaMemcpyHostToDevice, s_));
+	int rc0 = update_tile_hi();
+	if (rc0) return rc0;
 	uint32_t row = giter_ % w_.ring_rows;
 	PP_CK(cudaMemsetAsync(&w_.ring[(size_t) row * w_.nruns_cap + slot], 0, sizeof(PPStatistics), s_));
 	/* Grass of its tiles; its agents sorted by cell and appended to A. The
@@ -755,6 +780,7 @@ void World::release_pending()
 		}
 	}
 	if (!any) return;
+	update_tile_hi();
 	std::sort(free_tiles_.begin(), free_tiles_.end());
 	std::vector<std::pair<uint32_t, uint32_t>> merged;
 	for (auto &f : free_tiles_) {

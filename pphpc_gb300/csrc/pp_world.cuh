@@ -108,6 +108,8 @@ private:
 	/* Tiles of retired runs, with the world iteration of retirement. */
 	std::vector<std::pair<std::pair<uint32_t, uint32_t>, uint32_t>> pending_tiles_;
 	void release_pending();
+	int update_tile_hi();
+	uint32_t tile_hi_ = 0;    /* mirror of ctr->tile_hi */
 	uint32_t agents_reserved_ = 0;
 	uint32_t adm_used_ = 0;   /* admission area of the region buffer in use */
 	uint32_t fslot_base_ = 0; /* regrowth histograms of admitted runs start here */
