@@ -204,7 +204,8 @@ def measured_peaks():
 
 def ncu_traffic():
     """Per-launch DRAM traffic of each kernel from the committed ncu summary
-    (profiles/ncu_traffic.json), as bytes per processed unit."""
+    (profiles/ncu_traffic.json), as bytes per processed unit (agent, or
+    cell and agent), scaled to this workload."""
     try:
         with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
             return json.load(f)
@@ -256,6 +257,8 @@ def run_ours(args, dist):
         unit = tr.get("per")
         if unit == "agent":
             traffic = tr["bytes_per_unit"] * n_avg
+        elif unit == "cell+agent":
+            traffic = tr["bytes_per_cell"] * cells + tr["bytes_per_agent"] * n_avg
         elif unit == "launch":
             traffic = tr["bytes_per_launch"]
     step_bytes = sum(k[3] for k in kernels) / prof_iters
@@ -284,7 +287,7 @@ def run_ours(args, dist):
                    "init_sheep": p.init_sheep, "init_wolves": p.init_wolves,
                    "seed": SEED, "agent_pool": cap, "state": "uint32 SoA agents, uint16 grass",
                    "timed_iterations": "%d..%d" % (W + 1, W + K),
-                   "l2": "inputs larger than L2 (~1.6 GB working set)",
+                   "l2": "inputs larger than L2 (~2 GB working set)",
                    "parallelism": "replicas" if dist.world > 1 else "single"},
         "iters_per_s": iters_per_s,
         "e2e": {"value": e2e_value, "unit": "agent-steps/s",
