@@ -213,17 +213,32 @@ def ncu_traffic():
         return {}
 
 
+def workload(pp, args):
+    """The plain workload: 12800 x 12800 v1 by default; --side scales the
+    grid (agents by area) for smaller cases of the same kernels."""
+    if args.side == 12800:
+        return pp.make_params(**WORKLOAD), WORKLOAD_NAME
+    p = scaled_params(pp, args.side, 1, WORKLOAD["iters"])
+    return p, "pphpc-%dx%d-v1" % (args.side, args.side)
+
+
 def run_ours(args, dist):
     import pphpc_gb300 as pp
     pp.lib()
     dev = dist.local
-    p = pp.make_params(**WORKLOAD)
+    p, wname = workload(pp, args)
     n0 = p.init_sheep + p.init_wolves
     cap = 5 * n0
     K, W = args.steps, args.warmup
 
+    # -- launch geometry from the autotuner (or --tile-cells) --
+    tuning = None
+    if args.tile_cells == 0:
+        tuning = pp.autotune(p, SEED, cap, dev)
+
     # -- device-timed throughput (state resident in HBM) --
-    sim = pp.Simulation(p, SEED, device=dev, max_agents=cap)
+    sim = pp.Simulation(p, SEED, device=dev, max_agents=cap, tile_cells=args.tile_cells,
+                        autotune=args.tile_cells == 0)
     sim.step(W)
     clocks = ClockSampler(dev)
     clocks.start()
@@ -268,7 +283,8 @@ def run_ours(args, dist):
     # -- end to end through the C ABI with host buffers --
     dist.barrier()
     t0 = time.perf_counter()
-    sim2 = pp.Simulation(p, SEED, device=dev, max_agents=cap)
+    sim2 = pp.Simulation(p, SEED, device=dev, max_agents=cap, tile_cells=args.tile_cells,
+                         autotune=args.tile_cells == 0)
     rows0 = [sim2.stats0()]
     rows_e = sim2.step(K)
     h2d, d2h = sim2.io_bytes()
@@ -283,12 +299,13 @@ def run_ours(args, dist):
         "n_gpus": dist.world, "steps": K, "warmup": W,
         "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic (model's own seeded init)",
-        "config": {"workload": WORKLOAD_NAME, "grid": "12800x12800", "params": "v1",
+        "config": {"workload": wname, "grid": "%dx%d" % (p.grid_x, p.grid_y), "params": "v1",
                    "init_sheep": p.init_sheep, "init_wolves": p.init_wolves,
                    "seed": SEED, "agent_pool": cap, "state": "uint32 SoA agents, uint16 grass",
                    "timed_iterations": "%d..%d" % (W + 1, W + K),
                    "l2": "inputs larger than L2 (~2 GB working set)",
-                   "parallelism": "replicas" if dist.world > 1 else "single"},
+                   "parallelism": "replicas" if dist.world > 1 else "single",
+                   "geometry": tuning if tuning else {"tile_cells": args.tile_cells}},
         "iters_per_s": iters_per_s,
         "e2e": {"value": e2e_value, "unit": "agent-steps/s",
                 "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
@@ -337,14 +354,22 @@ def batched_vs_plain(args, dist):
             runs.append((scaled_params(pp, side, version, iters), seed))
             seed += 1
     dev = dist.local
+    # geometries from the autotuner, measured once per workload shape before
+    # the timed regions (the library caches them)
+    tune_b = pp.batch_autotune(runs, POOL_FACTOR, dev)
+    tune_p = {}
+    for p, sd in runs:
+        key = (p.grid_x, p.sheep_gain_from_food)
+        if key not in tune_p:
+            tune_p[key] = pp.autotune(p, sd, POOL_FACTOR * (p.init_sheep + p.init_wolves), dev)
     dist.barrier()
     t0 = time.perf_counter()
-    out_b = pp.batch_run(runs, pool_factor=POOL_FACTOR, device=dev)
+    out_b = pp.batch_run(runs, pool_factor=POOL_FACTOR, device=dev, autotune=True)
     t1 = time.perf_counter()
     out_p = []
     for p, sd in runs:
         n0 = p.init_sheep + p.init_wolves
-        out_p.append(pp.run(p, sd, device=dev, max_agents=POOL_FACTOR * n0))
+        out_p.append(pp.run(p, sd, device=dev, max_agents=POOL_FACTOR * n0, autotune=True))
     t2 = time.perf_counter()
     steps = 0
     exact = True
@@ -361,6 +386,9 @@ def batched_vs_plain(args, dist):
             "batched_agent_steps_per_s": steps_all / tb,
             "plain_agent_steps_per_s": steps_all / tp,
             "speedup": tp / tb, "bit_exact_batched_vs_plain": bool(exact),
+            "geometry_batched": tune_b,
+            "geometry_plain": {"%dx%d %s" % (k[0], k[0], "v1" if k[1] == 4 else "v2"): v
+                               for k, v in tune_p.items()},
             "timing": "wall clock, end to end through the C ABI (create, "
                       "iterations, stats rows to host, destroy)"}
 
@@ -460,6 +488,10 @@ def main():
                     help="iterations per run of the batched-vs-plain mix (0 = skip)")
     ap.add_argument("--workload", choices=["plain", "served"], default="plain")
     ap.add_argument("--served-requests", type=int, default=1000)
+    ap.add_argument("--side", type=int, default=12800,
+                    help="grid side of the plain workload (agents scale by area)")
+    ap.add_argument("--tile-cells", type=int, default=0,
+                    help="cells per act tile (0 = the library's choice)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

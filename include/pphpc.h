@@ -122,6 +122,9 @@ typedef struct pp_opts {
 	                           passes over the tile bits, tile offsets, act);
 	                           0 = fused act+move with a gather by destination
 	                           tile (default) */
+	uint32_t autotune;      /* 1 = when tile_cells is 0, measure the candidate
+	                           geometries (pp_autotune) and use the fastest;
+	                           0 = built-in choice */
 } pp_opts;
 
 /* Fill `opts` with defaults. */
@@ -266,6 +269,8 @@ typedef struct pp_batch_opts {
 	uint32_t sort_digit_bits; /* 0 = autotune */
 	uint32_t use_graph;     /* 1 = CUDA graph per iteration */
 	uint32_t stats_chunk;   /* iterations between stats copies to the host */
+	uint32_t autotune;      /* 1 = when tile_cells is 0, tune on the largest
+	                           run's parameters at the batch's pool density */
 } pp_batch_opts;
 
 void pp_batch_opts_default(pp_batch_opts *opts);
@@ -327,6 +332,32 @@ int pp_serve_load(pp_server *srv, uint32_t *queued, uint32_t *resident);
 int pp_serve_release(pp_server *srv, uint64_t id);
 
 int pp_serve_destroy(pp_server *srv);
+
+/* ------------------------------------------------------------------ */
+/* Autotuning (no counterpart in the reference, which takes its work   */
+/* sizes from command-line options: pp_gpu.c:310-410).                */
+/* ------------------------------------------------------------------ */
+
+typedef struct pp_tuning {
+	uint32_t tile_cells;        /* cells per act tile                      */
+	uint32_t sort_pipeline;     /* 1 = sort pipeline, 0 = fused            */
+	uint32_t sort_digit_bits;   /* 0 = the library's choice                */
+	float ns_per_agent_step;    /* measured device cost of the winner      */
+} pp_tuning;
+
+/* Measure the candidate geometries (fused and sort pipelines, 1024..8192
+ * cells per tile) on a sample of the workload -- the same parameters on at
+ * most 4096 x 4096 cells with agents and pool scaled by area -- and return
+ * the one with the lowest device time per agent-step. Results are cached
+ * per device and workload shape (and in the file named by PP_TUNE_CACHE,
+ * if set). `max_agents` is the pool the real run will use (0 = default). */
+int pp_autotune(const PPParameters *params, uint64_t seed, uint32_t max_agents,
+	int device, pp_tuning *out);
+
+/* The tuning pp_batch_run uses when opts->autotune is set: pp_autotune on
+ * the batch's largest run at the batch's pool density. */
+int pp_batch_autotune(const pp_run_desc *runs, int n_runs,
+	const pp_batch_opts *opts, pp_tuning *out);
 
 /* Library version string. */
 const char *pp_version(void);

@@ -74,7 +74,8 @@ class PPStatistics(C.Structure):
 class PPOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("max_agents", C.c_uint32),
                 ("tile_cells", C.c_uint32), ("sort_digit_bits", C.c_uint32),
-                ("use_graph", C.c_uint32), ("sort_pipeline", C.c_uint32)]
+                ("use_graph", C.c_uint32), ("sort_pipeline", C.c_uint32),
+                ("autotune", C.c_uint32)]
 
 
 class PPRunDesc(C.Structure):
@@ -84,7 +85,8 @@ class PPRunDesc(C.Structure):
 class PPBatchOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("pool_factor", C.c_uint32),
                 ("tile_cells", C.c_uint32), ("sort_digit_bits", C.c_uint32),
-                ("use_graph", C.c_uint32), ("stats_chunk", C.c_uint32)]
+                ("use_graph", C.c_uint32), ("stats_chunk", C.c_uint32),
+                ("autotune", C.c_uint32)]
 
 
 class PPServeOpts(C.Structure):
@@ -96,6 +98,11 @@ class PPServeOpts(C.Structure):
 class PPServeEvent(C.Structure):
     _fields_ = [("id", C.c_uint64), ("status", C.c_int),
                 ("n_rows", C.c_uint32), ("done", C.c_uint32)]
+
+
+class PPTuning(C.Structure):
+    _fields_ = [("tile_cells", C.c_uint32), ("sort_pipeline", C.c_uint32),
+                ("sort_digit_bits", C.c_uint32), ("ns_per_agent_step", C.c_float)]
 
 
 class KernelProf(C.Structure):
@@ -151,6 +158,9 @@ ABI = {
     "pp_serve_load": (C.c_int, [C.c_void_p, _u32p, _u32p]),
     "pp_serve_release": (C.c_int, [C.c_void_p, C.c_uint64]),
     "pp_serve_destroy": (C.c_int, [C.c_void_p]),
+    "pp_autotune": (C.c_int, [_P(PPParameters), C.c_uint64, C.c_uint32, C.c_int,
+                              _P(PPTuning)]),
+    "pp_batch_autotune": (C.c_int, [_P(PPRunDesc), C.c_int, _P(PPBatchOpts), _P(PPTuning)]),
     "pp_version": (C.c_char_p, []),
 }
 
@@ -212,7 +222,7 @@ class Simulation:
     """One PPHPC run on the GPU (pp_sim_* of the C ABI)."""
 
     def __init__(self, params, seed=0, device=0, max_agents=0, tile_cells=0,
-                 digit_bits=0, use_graph=True, sort_pipeline=False):
+                 digit_bits=0, use_graph=True, sort_pipeline=False, autotune=False):
         L = lib()
         o = PPOpts()
         L.pp_opts_default(C.byref(o))
@@ -222,6 +232,7 @@ class Simulation:
         o.sort_digit_bits = digit_bits
         o.use_graph = 1 if use_graph else 0
         o.sort_pipeline = 1 if sort_pipeline else 0
+        o.autotune = 1 if autotune else 0
         self.params = params
         self._h = C.c_void_p()
         _check(L.pp_sim_create(C.byref(params), seed, C.byref(o), C.byref(self._h)),
@@ -313,7 +324,7 @@ def run(params, seed=0, iters=None, **kw):
 
 
 def batch_run(runs, pool_factor=4, tile_cells=0, digit_bits=0, use_graph=True,
-              stats_chunk=1024, device=0):
+              stats_chunk=1024, device=0, autotune=False):
     """Run many independent simulations in one world. `runs` is a list of
     (PPParameters, seed); returns a list of row lists."""
     L = lib()
@@ -329,6 +340,7 @@ def batch_run(runs, pool_factor=4, tile_cells=0, digit_bits=0, use_graph=True,
     o.sort_digit_bits = digit_bits
     o.use_graph = 1 if use_graph else 0
     o.stats_chunk = stats_chunk
+    o.autotune = 1 if autotune else 0
     out = [None] * len(runs)
 
     def cb(r, rows, n, user):
@@ -401,6 +413,35 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def autotune(params, seed=0, max_agents=0, device=0):
+    """Measured launch geometry for a workload (pp_autotune): a dict with
+    tile_cells, sort_pipeline, sort_digit_bits, ns_per_agent_step."""
+    t = PPTuning()
+    _check(lib().pp_autotune(C.byref(params), seed, max_agents, device, C.byref(t)),
+           "pp_autotune")
+    return {"tile_cells": t.tile_cells, "sort_pipeline": bool(t.sort_pipeline),
+            "sort_digit_bits": t.sort_digit_bits,
+            "ns_per_agent_step": t.ns_per_agent_step}
+
+
+def batch_autotune(runs, pool_factor=4, device=0):
+    """The geometry batch_run(..., autotune=True) uses for these runs."""
+    descs = (PPRunDesc * len(runs))()
+    for i, (p, sd) in enumerate(runs):
+        descs[i].params = p
+        descs[i].seed = sd
+    o = PPBatchOpts()
+    lib().pp_batch_opts_default(C.byref(o))
+    o.device = device
+    o.pool_factor = pool_factor
+    t = PPTuning()
+    _check(lib().pp_batch_autotune(descs, len(runs), C.byref(o), C.byref(t)),
+           "pp_batch_autotune")
+    return {"tile_cells": t.tile_cells, "sort_pipeline": bool(t.sort_pipeline),
+            "sort_digit_bits": t.sort_digit_bits,
+            "ns_per_agent_step": t.ns_per_agent_step}
 
 
 def philox_fill(ctr, key, n):

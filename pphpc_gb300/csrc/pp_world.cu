@@ -845,6 +845,17 @@ extern "C" int pp_sim_create(const PPParameters *params, uint64_t seed,
 	cfg.digit_bits = o.sort_digit_bits;
 	cfg.graph_iters = o.use_graph ? 32 : 0;
 	cfg.fused = o.sort_pipeline == 0;
+	if (o.autotune && o.tile_cells == 0) {
+		pp_tuning tu;
+		rc = pp_autotune(&p, seed, cfg.cap, o.device, &tu);
+		if (rc) {
+			delete sim;
+			return rc;
+		}
+		cfg.tile_cells = tu.tile_cells;
+		cfg.fused = tu.sort_pipeline == 0;
+		if (tu.sort_digit_bits) cfg.digit_bits = tu.sort_digit_bits;
+	}
 	std::vector<RunSpec> runs(1);
 	runs[0].p = p;
 	runs[0].seed = seed;
@@ -1123,6 +1134,32 @@ extern "C" void pp_batch_opts_default(pp_batch_opts *o)
 	o->stats_chunk = 1024;
 }
 
+extern "C" int pp_batch_autotune(const pp_run_desc *runs, int n_runs,
+	const pp_batch_opts *opts, pp_tuning *out)
+{
+	/* tune on the run with the most cells, at the batch's pool density */
+	if (!runs || n_runs <= 0 || !out) return PP_INVALID_ARGS;
+	pp_batch_opts o;
+	if (opts) o = *opts;
+	else pp_batch_opts_default(&o);
+	uint64_t n0 = 0, cells = 0;
+	int big = 0;
+	for (int r = 0; r < n_runs; r++) {
+		const PPParameters &p = runs[r].params;
+		n0 += (uint64_t) p.init_sheep + p.init_wolves;
+		cells += (uint64_t) p.grid_x * p.grid_y;
+		if ((uint64_t) p.grid_x * p.grid_y
+			> (uint64_t) runs[big].params.grid_x * runs[big].params.grid_y) big = r;
+	}
+	const uint32_t pf = o.pool_factor ? o.pool_factor : 4;
+	const uint64_t cap = std::min<uint64_t>(std::max<uint64_t>(pf * n0, 1024), 0x7fffffffu);
+	PPParameters bp = runs[big].params;
+	bp.grid_xy = bp.grid_x * bp.grid_y;
+	const uint32_t bcap = (uint32_t) std::min<uint64_t>(0x7fffffffu,
+		(uint64_t) ((double) cap * bp.grid_xy / std::max<uint64_t>(cells, 1)) + 1024);
+	return pp_autotune(&bp, runs[big].seed, bcap, o.device, out);
+}
+
 extern "C" int pp_batch_run(const pp_run_desc *runs, int n_runs,
 	const pp_batch_opts *opts, pp_stats_cb cb, void *user)
 {
@@ -1152,6 +1189,14 @@ extern "C" int pp_batch_run(const pp_run_desc *runs, int n_runs,
 	cfg.tile_cells = o.tile_cells;
 	cfg.digit_bits = o.sort_digit_bits;
 	cfg.graph_iters = o.use_graph ? 32 : 0;
+	if (o.autotune && o.tile_cells == 0) {
+		pp_tuning tu;
+		int trc = pp_batch_autotune(runs, n_runs, &o, &tu);
+		if (trc) return trc;
+		cfg.tile_cells = tu.tile_cells;
+		cfg.fused = tu.sort_pipeline == 0;
+		if (tu.sort_digit_bits) cfg.digit_bits = tu.sort_digit_bits;
+	}
 	uint32_t chunk = o.stats_chunk ? o.stats_chunk : 1024;
 	cfg.ring_rows = std::max<uint32_t>(chunk + 1, 64);
 	World w;
