@@ -85,7 +85,7 @@ extern "C" int pp_serve_create(const pp_serve_opts *opts, pp_server **out)
 	 * (three key/value arrays for sorting a new run's agents, two group
 	 * buffers of three slots per agent, seven scratch words for crowded
 	 * tiles, sort look-back). Cells are bounded by the 2^31 key space. */
-	const uint32_t T = 2048;
+	const uint32_t T = 1024;
 	const uint64_t tile_bytes = T * 2ull + 610;
 	uint64_t budget = o.mem_budget_bytes;
 	uint64_t cell_bytes = budget / 8;
@@ -105,8 +105,9 @@ extern "C" int pp_serve_create(const pp_serve_opts *opts, pp_server **out)
 	cfg.nruns_cap = o.max_runs;
 	cfg.ring_rows = std::max<uint32_t>(o.stats_chunk + 1, 64);
 	cfg.graph_iters = 0;
-	/* Dense v2 runs put up to a few agents per cell in a tile. */
-	cfg.act_cap = 4096;
+	/* Dense v2 runs put up to ~2.2 agents per cell in a tile; tiles above
+	 * the shared-memory capacity take the act's crowded path. */
+	cfg.act_cap = 2048;
 	std::vector<RunSpec> none;
 	int rc = srv->world.create(none, cfg);
 	if (rc) {
@@ -134,7 +135,7 @@ extern "C" int pp_serve_submit(pp_server *srv, const pp_run_desc *run,
 	rq.spec.seed = run->seed;
 	rq.spec.iters = p.iters;
 	rq.reserve = reservation(rq.spec, srv->opts.pool_factor ? srv->opts.pool_factor : 4);
-	uint64_t tiles_needed = ((uint64_t) p.grid_xy + 2047) / 2048;
+	uint64_t tiles_needed = ((uint64_t) p.grid_xy + 1023) / 1024;
 	if (rq.reserve > srv->cap || tiles_needed > srv->max_tiles)
 		return PP_OUT_OF_RESOURCES; /* can never be admitted */
 	rq.rows.resize((size_t) p.iters + 1);
