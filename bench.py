@@ -36,6 +36,12 @@ With N > 1 (torchrun), every rank runs an independent replica (the runs
 do not exchange data); the timed region is bracketed by barriers and the
 slowest rank's time is used.
 
+  python bench.py --workload configs
+
+prints one line for the reference's two small plain configs (100^2 v1 seed
+0, 400^2 v2 seed 1, 4000 iterations), each run whole on the GPU and by the
+CPU restatement on all host threads.
+
   python bench.py --workload served
 
 prints one line for the served workload instead: a Poisson stream (20
@@ -393,6 +399,39 @@ def batched_vs_plain(args, dist):
                       "iterations, stats rows to host, destroy)"}
 
 
+def run_configs(args, dist):
+    """The reference's two small plain configs (100^2 v1 seed 0 and 400^2
+    v2 seed 1, 4000 iterations), each run whole on the GPU (end to end
+    through pp_sim_*, tuned geometry) and by the CPU restatement of the
+    reference's CPU algorithm on all host threads."""
+    import pphpc_gb300 as pp
+    from oracle import cpu_port
+    if dist.rank != 0:
+        return None
+    out = {"workload": "configs", "metric": "agent-steps/s", "unit": "agent-steps/s",
+           "n_gpus": 1, "configs": []}
+    for side, version, seed in ((100, 1, 0), (400, 2, 1)):
+        p = scaled_params(pp, side, version, 4000)
+        n0 = p.init_sheep + p.init_wolves
+        pp.autotune(p, seed, POOL_FACTOR * n0, dist.local)
+        t0 = time.perf_counter()
+        rows = pp.run(p, seed, device=dist.local, max_agents=POOL_FACTOR * n0, autotune=True)
+        tg = time.perf_counter() - t0
+        steps_g = sum(r.sheep + r.wolves for r in rows[:-1])
+        t0 = time.perf_counter()
+        crow = cpu_port.run(p, seed)
+        tc = time.perf_counter() - t0
+        steps_c = float(crow[:-1, 0].sum() + crow[:-1, 1].sum())
+        out["configs"].append({
+            "config": "%dx%d v%d seed %d, 4000 iterations" % (side, side, version, seed),
+            "gpu_agent_steps_per_s": steps_g / tg, "gpu_iters_per_s": 4000 / tg,
+            "cpu_agent_steps_per_s": steps_c / tc, "cpu_iters_per_s": 4000 / tc,
+            "cpu_cores": cpu_port.threads(), "cpu_kind": "port",
+            "timing": "wall clock of the whole run (GPU: create, 4000 iterations, "
+                      "stats to host, destroy)"})
+    return out
+
+
 def run_served(args, dist):
     """The served workload: Poisson arrivals into pp_serve_*; returns p50 /
     p99 completion latency and aggregate agent-steps/s."""
@@ -486,7 +525,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-iters", type=int, default=4000,
                     help="iterations per run of the batched-vs-plain mix (0 = skip)")
-    ap.add_argument("--workload", choices=["plain", "served"], default="plain")
+    ap.add_argument("--workload", choices=["plain", "served", "configs"], default="plain")
     ap.add_argument("--served-requests", type=int, default=1000)
     ap.add_argument("--side", type=int, default=12800,
                     help="grid side of the plain workload (agents scale by area)")
@@ -501,6 +540,8 @@ def main():
             out = run_reference(args, dist)
         elif args.workload == "served":
             out = run_served(args, dist)
+        elif args.workload == "configs":
+            out = run_configs(args, dist)
         else:
             out = run_ours(args, dist)
         if dist.rank == 0 and out is not None:
