@@ -184,9 +184,18 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 	}
 	const uint32_t g = w.ctr->giter + 1;
 	const uint32_t pin = g & 1, pout = ACT ? (g + 1) & 1 : g & 1;
-	const RunDev &run = w.runs[w.tile_run[tile]];
-	const uint32_t t = g - run.start_giter;
-	if (ACT && !run_live(run, t)) {
+	/* the run's parameters, copied to shared memory: they are read in every
+	 * phase, and through a reference into global memory they would be
+	 * reloaded after each global store (the compiler cannot rule out
+	 * aliasing) */
+	__shared__ RunDev s_run;
+	const RunDev &grun = w.runs[w.tile_run[tile]];
+	static_assert(sizeof(RunDev) % 4 == 0 && sizeof(RunDev) / 4 <= NT, "run copy");
+	if (tid < sizeof(RunDev) / 4)
+		reinterpret_cast<uint32_t *>(&s_run)[tid] = reinterpret_cast<const uint32_t *>(&grun)[tid];
+	const RunDev &run = s_run;
+	const uint32_t t = g - grun.start_giter;
+	if (ACT && !run_live(grun, t)) {
 		cp_async_wait_all();
 		/* finished run or free tile space: nothing survives, no stats */
 		if (tid == 0) w.inbox_n[(size_t) pin * w.n_tiles + tile] = 0;
@@ -194,9 +203,9 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		return;
 	}
 	const uint32_t tmove = ACT ? t + 1 : t;
-	const bool live_move = run_live(run, tmove);
-	const uint32_t seed_lo = run.seed_lo, seed_hi = run.seed_hi;
-	const uint32_t lt0 = c0 - run.cbase;          /* run-local index of the tile start */
+	const bool live_move = run_live(grun, tmove);
+	const uint32_t seed_lo = grun.seed_lo, seed_hi = grun.seed_hi;
+	const uint32_t lt0 = c0 - grun.cbase;         /* run-local index of the tile start */
 	const uint32_t lcmask = (1u << w.log_tile) - 1;
 	if (tid < CLS_FOREIGN) s_tbl[tid] = TBL_EMPTY;
 	if (tid <= NCLS) s_ccnt[tid] = 0;
