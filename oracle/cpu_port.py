@@ -33,8 +33,9 @@ class PStats(C.Structure):
 
 
 def build():
+    from pphpc_gb300.build import native_ok
     os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
-    if (not os.path.exists(LIB_PATH)
+    if (not os.path.exists(LIB_PATH) or not native_ok(LIB_PATH)
             or os.path.getmtime(LIB_PATH) < os.path.getmtime(SRC)):
         subprocess.run(["gcc", "-O2", "-std=gnu11", "-fopenmp", "-fPIC", "-shared",
                         "-Wall", "-o", LIB_PATH, SRC], check=True)

@@ -40,8 +40,8 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            from pphpc_gb300 import build as _b  # builds oracle/_build too
+        from pphpc_gb300 import build as _b  # builds oracle/_build too
+        if not os.path.exists(LIB_PATH) or not _b.native_ok(LIB_PATH):
             _b.build_oracle()
         L = C.CDLL(LIB_PATH)
         L.ppo_philox.argtypes = [_u32p, _u32p, _u32p]

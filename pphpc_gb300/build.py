@@ -31,9 +31,31 @@ HEADERS = ["pp_device.cuh", "pp_kernels.cuh", "pp_block.cuh", "pp_world.cuh",
            "pp_act.cuh"]
 
 
+_ELF_MACHINE = {"x86_64": 62, "aarch64": 183, "arm64": 183}
+
+
+def native_ok(path):
+    """True if `path` is an ELF file built for this machine's architecture
+    (a binary copied from another architecture, or an emptied one, is not)."""
+    import platform
+    import struct
+    try:
+        with open(path, "rb") as f:
+            head = f.read(20)
+    except OSError:
+        return False
+    if len(head) < 20 or head[:4] != b"\x7fELF":
+        return False
+    want = _ELF_MACHINE.get(platform.machine())
+    return want is None or struct.unpack("<H", head[18:20])[0] == want
+
+
 def _newer(target, deps):
     if not os.path.exists(target):
         return True
+    if target.endswith((".o", ".so")) or os.access(target, os.X_OK):
+        if not native_ok(target):
+            return True
     t = os.path.getmtime(target)
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
@@ -89,6 +111,10 @@ def build_oracle():
 def build_all(verbose=False):
     lib = build_library(verbose=verbose)
     build_oracle()
+    # the CPU restatement of the reference's algorithm (test infrastructure)
+    sys.path.insert(0, ROOT)
+    from oracle import cpu_port
+    cpu_port.build()
     return lib
 
 

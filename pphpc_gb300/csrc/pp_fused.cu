@@ -480,13 +480,17 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		en = nb ? LD[j] : (LV[j] & ENERGY_MASK);
 	};
 
-	/* ---- E1: move draws of the outputs, per-class counts ---- */
+	/* ---- E1: move draws of the outputs, per-class counts; with room in
+	 * the cell counters' words (2 act_cap <= T), each output's key bits and
+	 * class are kept for E2, else only its direction ---- */
 	bool bad = false;
+	const bool cache = in_smem && 2u * w.act_cap <= (uint32_t) (CPT * NT);
+	uint32_t *DEST = scnt;
 	for (uint32_t o = tid; o < total; o += NT) {
 		uint32_t j, nb, en, rank;
 		output(o, j, nb, en, rank);
 		const uint32_t lc = LK[j];
-		uint32_t code, cls;
+		uint32_t code, cls, klo = lc;
 		if (!live_move) {
 			code = DIR_PARKED;
 			cls = CLS_GRAVE;
@@ -496,14 +500,17 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		} else {
 			const u4 r = rng(seed_lo, seed_hi, lt0 + lc, tmove, STREAM_MOVE, rank);
 			code = draw(r.x, 5);
-			const uint32_t dt = (run.cbase + move_dir(run, lt0 + lc, code)) >> w.log_tile;
+			const uint32_t dg = run.cbase + move_dir(run, lt0 + lc, code);
+			const uint32_t dt = dg >> w.log_tile;
+			klo = dg & lcmask;
 			cls = dt == tile ? CLS_OWN : class_insert(s_tbl, dt);
 		}
-		DIR[o] = (uint8_t) code;
 		if (cls == CLS_NONE || rank > REC_RANK_MAX) {
 			bad = true;
 			cls = NCLS;                      /* counted nowhere */
 		}
+		if (cache) DEST[o] = klo | (code << REC_DIR_SHIFT) | (cls << 16);
+		else DIR[o] = (uint8_t) code;
 		warp_agg_add(s_ccnt, cls);
 	}
 	if (bad) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
@@ -548,8 +555,21 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 			output(o, j, nb, en, rank);
 			const uint32_t lc = LK[j];
 			const uint32_t tb = LV[j] & TYPE_BIT;
-			const uint32_t code = DIR[o];
 			uint32_t key, val, cls;
+			if (cache) {
+				const uint32_t d = DEST[o];
+				const uint32_t code = (d >> REC_DIR_SHIFT) & 7u;
+				cls = d >> 16;
+				key = (d & 0xffffu) | (rank << REC_RANK_SHIFT);
+				val = code >= DIR_PARKED ? (tb | en) : (tb | (en - 1));
+				const uint32_t pos = warp_agg_add(s_cpos, cls);
+				if (cls != NCLS) {
+					kGo[pos] = key;
+					vGo[pos] = val;
+				}
+				continue;
+			}
+			const uint32_t code = DIR[o];
 			if (code >= DIR_PARKED) {
 				cls = CLS_GRAVE;
 				key = lc | (code << REC_DIR_SHIFT) | (rank << REC_RANK_SHIFT);
