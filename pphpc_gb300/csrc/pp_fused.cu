@@ -35,7 +35,10 @@ namespace {
 
 static_assert(IBX == 32, "the inbox is read by one warp");
 
-constexpr int NT = 128;                 /* threads per tile CTA (eight CTAs per SM) */
+/* Threads per tile CTA: 128 for sparse tiles (eight CTAs per SM), 256 when
+ * a tile may hold more agents than half its cells (its shared memory then
+ * limits the SM to about four CTAs). */
+constexpr int NT_SPARSE = 128, NT_DENSE = 256;
 constexpr uint32_t NCLS = 32;          /* group classes of a tile (one per lane) */
 constexpr uint32_t CLS_FOREIGN = 30;   /* classes 0..29: other destination tiles */
 constexpr uint32_t CLS_OWN = 30;       /* moved within the tile                  */
@@ -114,6 +117,7 @@ __device__ __forceinline__ int64_t order_key(uint32_t rec, uint32_t x,
 
 /* Exclusive scan of one value per thread over the NT threads of the CTA;
  * the total goes to *total. */
+template <int NT>
 __device__ __forceinline__ uint32_t step_excl_scan(uint32_t v, uint32_t *total)
 {
 	__shared__ uint32_t ws[NT / 32];
@@ -138,7 +142,7 @@ __device__ __forceinline__ uint32_t step_excl_scan(uint32_t v, uint32_t *total)
 	return before + x - v;
 }
 
-/* One CTA per tile of CPT * NT cells.
+/* One CTA of NT threads per tile of CPT * NT cells.
  *   ACT:  the act of iteration t of the tile's agents (gathered from its
  *         inbox of parity t) and the move of iteration t + 1 of its
  *         survivors and newborns into the group buffer of parity t + 1.
@@ -149,7 +153,7 @@ __device__ __forceinline__ uint32_t step_excl_scan(uint32_t v, uint32_t *total)
  * act); E0 output offsets and stats; E1 move draws and per-class counts;
  * one warp allocates the tile's groups and posts them to the destination
  * tiles' inboxes; E2 records into the groups; per-tile stats. */
-template <int CPT, bool ACT>
+template <int CPT, int NT, bool ACT>
 __device__ __forceinline__ void step_tile(const WorldDev &w,
 	const uint32_t *__restrict__ kS, const uint32_t *__restrict__ vS,
 	uint32_t tile, uint32_t out_base, uint32_t *sm)
@@ -332,7 +336,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 				if (c > 1) multi |= 1ull << q;
 			}
 			uint32_t tot;
-			uint32_t run_start = step_excl_scan(loc, &tot);
+			uint32_t run_start = step_excl_scan<NT>(loc, &tot);
 #pragma unroll
 			for (int q = 0; q < CPT; q++) {
 				const uint32_t c = scnt[q * NT + tid];
@@ -436,7 +440,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 	uint8_t *DIR = in_smem ? reinterpret_cast<uint8_t *>(scnt)
 		: reinterpret_cast<uint8_t *>(PERM + 2 * m);
 	if (ACT) {
-		uint32_t o = step_excl_scan(cnt, &total);
+		uint32_t o = step_excl_scan<NT>(cnt, &total);
 		for (uint32_t j = ja; j < jb; j++) {
 			LP[j] = o;
 			if (LV[j] & ENERGY_MASK) {
@@ -632,23 +636,38 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 /* The fused act: one CTA per tile below the world's high-water mark (the
  * host sizes the grid from it and moves it when runs are admitted or
  * retired), so a serving world's free tile space costs nothing. */
-template <int CPT>
-__global__ void __launch_bounds__(NT, 8) k_step_act(WorldDev w)
+template <int CPT, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_step_act(WorldDev w)
 {
 	extern __shared__ __align__(16) uint32_t sm[];
 	if (blockIdx.x >= min(w.ctr->tile_hi, w.n_tiles)) return;
-	step_tile<CPT, true>(w, nullptr, nullptr, blockIdx.x, 0, sm);
+	step_tile<CPT, NT, true>(w, nullptr, nullptr, blockIdx.x, 0, sm);
 }
 
 /* The first move of a freshly initialised run: one CTA per tile of
  * [tile0, tile0 + gridDim.x). */
-template <int CPT>
-__global__ void __launch_bounds__(NT, 8) k_step_first(WorldDev w,
+template <int CPT, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_step_first(WorldDev w,
 	const uint32_t *__restrict__ kS, const uint32_t *__restrict__ vS,
 	uint32_t tile0, uint32_t out_base)
 {
 	extern __shared__ __align__(16) uint32_t sm[];
-	step_tile<CPT, false>(w, kS, vS, tile0 + blockIdx.x, out_base, sm);
+	step_tile<CPT, NT, false>(w, kS, vS, tile0 + blockIdx.x, out_base, sm);
+}
+
+template <int CPT, int NT, bool ACT>
+void launch_one(const WorldDev &w, uint32_t grid, size_t smem,
+	const uint32_t *k, const uint32_t *v, uint32_t first, uint32_t out_base,
+	cudaStream_t s)
+{
+	if (ACT) k_step_act<CPT, NT><<<grid, NT, smem, s>>>(w);
+	else k_step_first<CPT, NT><<<grid, NT, smem, s>>>(w, k, v, first, out_base);
+}
+
+/* Thread count of a world's tile CTAs (see NT_SPARSE / NT_DENSE). */
+inline int step_threads(const WorldDev &w)
+{
+	return 2u * w.act_cap > (1u << w.log_tile) ? NT_DENSE : NT_SPARSE;
 }
 
 template <bool ACT>
@@ -659,45 +678,33 @@ cudaError_t launch_step(const WorldDev &w, const LaunchCfg &lc,
 	const uint32_t T = 1u << w.log_tile;
 	const size_t smem = (size_t) w.act_cap * 5 * sizeof(uint32_t)
 		+ (size_t) T * (sizeof(uint32_t) + sizeof(uint16_t));
-	if (ACT) {
-		const uint32_t grid = (uint32_t) std::max(1, lc.act_tiles);
-		switch (T / NT) {
-		case 8: k_step_act<8><<<grid, NT, smem, s>>>(w); break;
-		case 16: k_step_act<16><<<grid, NT, smem, s>>>(w); break;
-		case 32: k_step_act<32><<<grid, NT, smem, s>>>(w); break;
-		default: k_step_act<64><<<grid, NT, smem, s>>>(w); break;
+	const uint32_t grid = ACT ? (uint32_t) std::max(1, lc.act_tiles) : count;
+	if (step_threads(w) == NT_DENSE) {
+		switch (T / NT_DENSE) {
+		case 4: launch_one<4, NT_DENSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
+		case 8: launch_one<8, NT_DENSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
+		case 16: launch_one<16, NT_DENSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
+		default: launch_one<32, NT_DENSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
 		}
 	} else {
-		switch (T / NT) {
-		case 8: k_step_first<8><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
-		case 16: k_step_first<16><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
-		case 32: k_step_first<32><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
-		default: k_step_first<64><<<count, NT, smem, s>>>(w, k, v, first, out_base); break;
+		switch (T / NT_SPARSE) {
+		case 8: launch_one<8, NT_SPARSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
+		case 16: launch_one<16, NT_SPARSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
+		case 32: launch_one<32, NT_SPARSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
+		default: launch_one<64, NT_SPARSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
 		}
 	}
 	return cudaGetLastError();
 }
 
-template <int CPT>
+template <int CPT, int NT>
 cudaError_t set_step_limit(size_t bytes)
 {
-	cudaError_t e = cudaFuncSetAttribute(k_step_act<CPT>,
+	cudaError_t e = cudaFuncSetAttribute(k_step_act<CPT, NT>,
 		cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
 	if (e != cudaSuccess) return e;
-	return cudaFuncSetAttribute(k_step_first<CPT>,
+	return cudaFuncSetAttribute(k_step_first<CPT, NT>,
 		cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
-}
-
-template <int CPT>
-int step_occupancy(size_t smem)
-{
-	int n = 0;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_act<CPT>, NT, smem)
-		!= cudaSuccess) {
-		cudaGetLastError();
-		return 1;
-	}
-	return n;
 }
 
 } /* namespace */
@@ -724,22 +731,16 @@ cudaError_t enqueue_move_groups(const WorldDev &w, const LaunchCfg &lc,
 	return launch_step<false>(w, lc, k, v, first, count, out_base, s);
 }
 
-int occupancy_step(uint32_t tile_cells, size_t smem)
-{
-	switch (tile_cells / NT) {
-	case 8: return step_occupancy<8>(smem);
-	case 16: return step_occupancy<16>(smem);
-	case 32: return step_occupancy<32>(smem);
-	default: return step_occupancy<64>(smem);
-	}
-}
-
 cudaError_t set_step_smem_limits(size_t bytes)
 {
-	cudaError_t e = set_step_limit<8>(bytes);
-	if (e == cudaSuccess) e = set_step_limit<16>(bytes);
-	if (e == cudaSuccess) e = set_step_limit<32>(bytes);
-	if (e == cudaSuccess) e = set_step_limit<64>(bytes);
+	cudaError_t e = set_step_limit<8, NT_SPARSE>(bytes);
+	if (e == cudaSuccess) e = set_step_limit<16, NT_SPARSE>(bytes);
+	if (e == cudaSuccess) e = set_step_limit<32, NT_SPARSE>(bytes);
+	if (e == cudaSuccess) e = set_step_limit<64, NT_SPARSE>(bytes);
+	if (e == cudaSuccess) e = set_step_limit<4, NT_DENSE>(bytes);
+	if (e == cudaSuccess) e = set_step_limit<8, NT_DENSE>(bytes);
+	if (e == cudaSuccess) e = set_step_limit<16, NT_DENSE>(bytes);
+	if (e == cudaSuccess) e = set_step_limit<32, NT_DENSE>(bytes);
 	return e;
 }
 

@@ -85,7 +85,6 @@ cudaError_t enqueue_fused_bases(const WorldDev &w, const LaunchCfg &lc,
 	cudaStream_t s);
 
 cudaError_t set_step_smem_limits(size_t bytes);
-int occupancy_step(uint32_t tile_cells, size_t smem);
 
 /* Initialisation of a run: grass of its tiles; its initial agents in
  * creation order into k/v[base ..) (sorted by cell afterwards); the stats
