@@ -118,3 +118,12 @@ def test_invariants_long_run():
     assert np.all(rows[:, 2] <= cells)
     assert np.all(rows[:, 5] <= cells * restart)
     assert np.all((rows[:, 0] == 0) | (rows[:, 3] >= rows[:, 0]))
+
+
+@pytest.mark.parametrize("tile", [1024, 2048, 4096])
+@pytest.mark.parametrize("side,version,seed,iters,pool", [
+    (200, 1, 3, 300, 12000), (256, 1, 8, 200, 20000), (160, 2, 5, 30, 16000)])
+def test_sparse_tiles_bit_exact(side, version, seed, iters, pool, tile):
+    # a pool of well under one agent per cell: the act runs 128-thread CTAs
+    # (sparse tiles) instead of the 256-thread ones the other tests get
+    _check_run(params(side, version), seed, iters, max_agents=pool, tile_cells=tile)
