@@ -499,15 +499,21 @@ def run_reference(args, dist):
     if dist.rank != 0:
         return None
     from oracle import cpu_port
-    r = cpu_port.run_steps(WORKLOAD, SEED, args.steps, args.warmup)
+    wl, wname = dict(WORKLOAD), WORKLOAD_NAME
+    if args.side != 12800:
+        a = args.side * args.side
+        wl.update(grid_x=args.side, grid_y=args.side, init_sheep=a * 4 // 100,
+                  init_wolves=a * 2 // 100)
+        wname = "pphpc-%dx%d-v1" % (args.side, args.side)
+    r = cpu_port.run_steps(wl, SEED, args.steps, args.warmup)
     return {
         "impl": "reference", "metric": "agent-steps/s", "value": r["value"],
         "unit": "agent-steps/s", "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic (model's own seeded init)",
-        "config": {"workload": WORKLOAD_NAME, "grid": "12800x12800", "params": "v1",
-                   "seed": SEED},
+        "config": {"workload": wname, "grid": "%dx%d" % (wl["grid_x"], wl["grid_y"]),
+                   "params": "v1", "seed": SEED},
         "cpu_baseline": {"value": r["value"], "unit": "agent-steps/s",
                          "cores": r["cores"], "kind": "port", "sample": r["sample"]},
         "e2e": {"value": r["value"], "unit": "agent-steps/s",
