@@ -197,6 +197,21 @@ int pp_sim_io_bytes(pp_sim *sim, uint64_t *h2d, uint64_t *d2h);
 /* The cudaStream_t the simulation runs on (as void*). */
 void *pp_sim_stream(pp_sim *sim);
 
+/* Write the simulation's state after its last iteration -- agents in
+ * canonical order (run-local cell, type << 31 | energy), grass countdowns,
+ * the iteration number, parameters and seed -- to the file `path`. A
+ * simulation restored from it continues with exactly the stats and state
+ * of the uninterrupted one (every draw is keyed by cell, iteration and
+ * rank, none by memory layout). No counterpart in the reference (SURVEY
+ * §8(f): state snapshot / resume). */
+int pp_sim_snapshot_save(pp_sim *sim, const char *path);
+
+/* Create a simulation from a snapshot file written by pp_sim_snapshot_save.
+ * pp_sim_stats0 returns the stats of the saved state and pp_sim_info the
+ * saved iteration plus the iterations run since. PP_INVALID_PARAMS_FILE if
+ * the file is not a snapshot. */
+int pp_sim_restore(const char *path, const pp_opts *opts, pp_sim **out);
+
 int pp_sim_destroy(pp_sim *sim);
 
 /* ------------------------------------------------------------------ */

@@ -137,6 +137,8 @@ ABI = {
                                      _P(PPStatistics)]),
     "pp_sim_io_bytes": (C.c_int, [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)]),
     "pp_sim_destroy": (C.c_int, [C.c_void_p]),
+    "pp_sim_snapshot_save": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "pp_sim_restore": (C.c_int, [C.c_char_p, _P(PPOpts), _P(C.c_void_p)]),
     "pp_philox_fill": (C.c_int, [C.c_uint32] * 7 + [_u32p]),
     "pp_move_host": (C.c_int, [_P(PPParameters), C.c_uint64, C.c_uint32, C.c_uint32,
                                _u32p, _u32p, _u32p, _u32p]),
@@ -222,7 +224,8 @@ class Simulation:
     """One PPHPC run on the GPU (pp_sim_* of the C ABI)."""
 
     def __init__(self, params, seed=0, device=0, max_agents=0, tile_cells=0,
-                 digit_bits=0, use_graph=True, sort_pipeline=False, autotune=False):
+                 digit_bits=0, use_graph=True, sort_pipeline=False, autotune=False,
+                 _restore=None):
         L = lib()
         o = PPOpts()
         L.pp_opts_default(C.byref(o))
@@ -235,8 +238,24 @@ class Simulation:
         o.autotune = 1 if autotune else 0
         self.params = params
         self._h = C.c_void_p()
-        _check(L.pp_sim_create(C.byref(params), seed, C.byref(o), C.byref(self._h)),
-               "pp_sim_create")
+        if _restore is not None:
+            _check(L.pp_sim_restore(os.fsencode(_restore), C.byref(o), C.byref(self._h)),
+                   "pp_sim_restore")
+        else:
+            _check(L.pp_sim_create(C.byref(params), seed, C.byref(o), C.byref(self._h)),
+                   "pp_sim_create")
+
+    @classmethod
+    def restore(cls, path, params, **kw):
+        """A simulation continuing from a snapshot file (pp_sim_restore);
+        `params` must be the saved simulation's parameters (the file holds
+        them; they size the Python-side buffers)."""
+        return cls(params, _restore=path, **kw)
+
+    def save(self, path):
+        """Write a snapshot of the current state (pp_sim_snapshot_save)."""
+        _check(lib().pp_sim_snapshot_save(self._h, os.fsencode(path)),
+               "pp_sim_snapshot_save")
 
     def stats0(self):
         s = PPStatistics()

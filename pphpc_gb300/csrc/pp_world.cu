@@ -123,7 +123,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	uint64_t total_cells = 0, n0 = 0;
 	for (const RunSpec &r : runs) {
 		total_cells += (uint64_t) r.p.grid_x * r.p.grid_y;
-		n0 += (uint64_t) r.p.init_sheep + r.p.init_wolves;
+		n0 += r.agents();
 	}
 	if (cfg.cap == 0) cfg.cap = (uint32_t) std::min<uint64_t>(
 		std::max<uint64_t>(4 * n0, 1024), 0x7fffffffu);
@@ -249,10 +249,13 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	std::vector<uint32_t> base_h(nruns_cap, 0);
 	uint32_t base = 0;
 	for (size_t r = 0; r < runs.size(); r++) {
-		runs_h_[r] = make_run(runs[r], first[r], ntl[r], log_tile, 0, fbase_h[r]);
+		/* a resumed run's iteration t is the world's iteration plus its
+		 * start iteration (unsigned wrap-around) */
+		runs_h_[r] = make_run(runs[r], first[r], ntl[r], log_tile,
+			0u - runs[r].start_iter, fbase_h[r]);
 		for (uint32_t t = 0; t < ntl[r]; t++) tile_run_h_[first[r] + t] = (uint16_t) r;
 		base_h[r] = base;
-		base += runs[r].p.init_sheep + runs[r].p.init_wolves;
+		base += (uint32_t) runs[r].agents();
 	}
 	if (cfg.extra_tiles) free_tiles_.push_back({used_tiles_, cfg.extra_tiles});
 	PP_CK(cudaMemcpyAsync(w_.runs, runs_h_.data(), nruns_cap * sizeof(RunDev), cudaMemcpyHostToDevice, s_));
@@ -281,7 +284,13 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	 * B at the run's base, sorted by cell into the region buffer (runs
 	 * occupy increasing cell ranges, so each run's agents stay at its
 	 * base), the tiles' regions and dense bases, stats row 0. */
+	std::vector<PPStatistics> resumed_row0(runs.size());
 	for (size_t r = 0; r < runs.size(); r++) {
+		if (runs[r].init_val) {
+			rc = load_run_state(runs[r], runs_h_[r], base_h[r], &resumed_row0[r]);
+			if (rc) return rc;
+			continue;
+		}
 		rc = cuda_status(enqueue_init_grass(w_, runs_h_[r], s_));
 		if (rc) return rc;
 		rc = cuda_status(enqueue_init_agents(runs_h_[r], w_.kB, w_.vB, base_h[r],
@@ -305,6 +314,12 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 		sorted_v = w_.vR;
 	}
 	for (size_t r = 0; r < runs.size(); r++) {
+		if (runs[r].init_val) {
+			PP_CK(cudaMemcpyAsync(&w_.ring[r], &resumed_row0[r], sizeof(PPStatistics),
+				cudaMemcpyHostToDevice, s_));
+			h2d_ += sizeof(PPStatistics);
+			continue;
+		}
 		rc = cuda_status(enqueue_stats_run(w_, runs_h_[r], (uint32_t) r,
 			sorted_v + base_h[r], runs[r].p.init_sheep + runs[r].p.init_wolves, 0, s_));
 		if (rc) return rc;
@@ -316,6 +331,53 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 		rc = build_graph();
 		if (rc) return rc;
 	}
+	return PP_SUCCESS;
+}
+
+int World::load_run_state(const RunSpec &spec, const RunDev &run, uint32_t base,
+	PPStatistics *row0)
+{
+	/* A resumed run: its agents (run-local cells, canonical order) into B at
+	 * its base; its grass as regrowth iterations start_iter + countdown,
+	 * each pending regrowth counted in the run's histogram; the stats of
+	 * the state as its row 0. */
+	const uint32_t n = spec.init_n, cells = run.ncells, T0 = spec.start_iter;
+	const uint32_t fs = run.restart + 1;
+	std::vector<uint32_t> kc(n);
+	PPStatistics st{};
+	for (uint32_t i = 0; i < n; i++) {
+		if (spec.init_cell[i] >= cells) return PP_INVALID_ARGS;
+		if (i && spec.init_cell[i] < spec.init_cell[i - 1]) return PP_INVALID_ARGS;
+		const uint32_t v = spec.init_val[i], e = v & ENERGY_MASK;
+		if (e == 0) return PP_INVALID_ARGS;
+		kc[i] = run.cbase + spec.init_cell[i];
+		if (v & TYPE_BIT) { st.wolves++; st.wolves_en += e; }
+		else { st.sheep++; st.sheep_en += e; }
+	}
+	std::vector<uint16_t> g(cells);
+	std::vector<uint32_t> hist(fs, 0);
+	for (uint32_t c = 0; c < cells; c++) {
+		const uint32_t cd = spec.init_grass[c];
+		if (cd > run.restart) return PP_INVALID_ARGS;
+		g[c] = (uint16_t) (T0 + cd);
+		if (cd) hist[(T0 + cd) % fs]++;
+		else st.grass++;
+		st.grass_en += cd;
+	}
+	*row0 = st;
+	if (n) {
+		PP_CK(cudaMemcpyAsync(w_.kB + base, kc.data(), (size_t) n * 4, cudaMemcpyHostToDevice, s_));
+		PP_CK(cudaMemcpyAsync(w_.vB + base, spec.init_val, (size_t) n * 4, cudaMemcpyHostToDevice, s_));
+	}
+	PP_CK(cudaMemsetAsync(w_.grass + run.cbase, 0,
+		((size_t) run.n_tiles << w_.log_tile) * sizeof(uint16_t), s_));
+	PP_CK(cudaMemcpyAsync(w_.grass + run.cbase, g.data(), (size_t) cells * 2,
+		cudaMemcpyHostToDevice, s_));
+	PP_CK(cudaMemcpyAsync(w_.fring + run.fbase, hist.data(), (size_t) fs * 4,
+		cudaMemcpyHostToDevice, s_));
+	/* the host vectors go out of scope: wait for the copies */
+	PP_CK(cudaStreamSynchronize(s_));
+	h2d_ += (uint64_t) n * 8 + (uint64_t) cells * 2 + (uint64_t) fs * 4;
 	return PP_SUCCESS;
 }
 
@@ -806,6 +868,7 @@ struct pp_sim {
 	PPParameters params;
 	uint64_t seed;
 	PPStatistics stats0;
+	uint32_t iter0 = 0;     /* iteration the simulation was restored at */
 };
 
 extern "C" void pp_opts_default(pp_opts *o)
@@ -819,8 +882,10 @@ extern "C" void pp_opts_default(pp_opts *o)
 	o->sort_pipeline = 0;
 }
 
-extern "C" int pp_sim_create(const PPParameters *params, uint64_t seed,
-	const pp_opts *opts, pp_sim **out)
+/* A simulation from parameters and a seed, or from a saved state (spec0's
+ * init arrays and start iteration). */
+static int sim_create(const PPParameters *params, uint64_t seed,
+	const pp_opts *opts, const RunSpec *spec0, pp_sim **out)
 {
 	if (!params || !out) return PP_INVALID_ARGS;
 	*out = nullptr;
@@ -838,6 +903,7 @@ extern "C" int pp_sim_create(const PPParameters *params, uint64_t seed,
 	WorldConfig cfg;
 	cfg.device = o.device;
 	uint64_t n0 = (uint64_t) p.init_sheep + p.init_wolves;
+	if (spec0) n0 = std::max<uint64_t>(n0, spec0->init_n);
 	uint64_t cap = o.max_agents ? o.max_agents
 		: std::max<uint64_t>(std::max<uint64_t>(4 * n0, 1024), 16777216ull);
 	cfg.cap = (uint32_t) std::min<uint64_t>(cap, 0x7fffffffu);
@@ -857,9 +923,11 @@ extern "C" int pp_sim_create(const PPParameters *params, uint64_t seed,
 		if (tu.sort_digit_bits) cfg.digit_bits = tu.sort_digit_bits;
 	}
 	std::vector<RunSpec> runs(1);
+	if (spec0) runs[0] = *spec0;
 	runs[0].p = p;
 	runs[0].seed = seed;
 	runs[0].iters = 0xffffffffu;
+	sim->iter0 = spec0 ? spec0->start_iter : 0;
 	rc = sim->world.create(runs, cfg);
 	if (rc == PP_SUCCESS) rc = sim->world.read_rows(0, 0, 0, &sim->stats0);
 	if (rc) {
@@ -869,6 +937,82 @@ extern "C" int pp_sim_create(const PPParameters *params, uint64_t seed,
 	}
 	*out = sim;
 	return PP_SUCCESS;
+}
+
+extern "C" int pp_sim_create(const PPParameters *params, uint64_t seed,
+	const pp_opts *opts, pp_sim **out)
+{
+	return sim_create(params, seed, opts, nullptr, out);
+}
+
+/* Snapshot file: magic, parameters, seed, iteration, agent count, then the
+ * agents' run-local cells and type | energy words in canonical order and
+ * the grid's grass countdowns (native byte order). */
+static const char SNAP_MAGIC[8] = {'P', 'P', 'S', 'N', 'A', 'P', '0', '1'};
+
+extern "C" int pp_sim_snapshot_save(pp_sim *sim, const char *path)
+{
+	if (!sim || !path) return PP_INVALID_ARGS;
+	World &w = sim->world;
+	uint32_t n = 0;
+	int rc = w.get_state(nullptr, nullptr, 0, &n, nullptr, 0);
+	if (rc) return rc;
+	const PPParameters &p = sim->params;
+	std::vector<uint32_t> cell(std::max<uint32_t>(n, 1)), en(std::max<uint32_t>(n, 1));
+	std::vector<uint16_t> grass((size_t) p.grid_x * p.grid_y);
+	uint32_t n2 = 0;
+	rc = w.get_state(cell.data(), en.data(), n, &n2, grass.data(), 0);
+	if (rc) return rc;
+	if (n2 != n) return PP_LIBRARY_ERROR;
+	const uint32_t iter = sim->iter0 + w.giter();
+	FILE *f = fopen(path, "wb");
+	if (!f) return PP_UNABLE_SAVE_STATS;
+	bool ok = fwrite(SNAP_MAGIC, 1, 8, f) == 8
+		&& fwrite(&p, sizeof(p), 1, f) == 1
+		&& fwrite(&sim->seed, 8, 1, f) == 1
+		&& fwrite(&iter, 4, 1, f) == 1
+		&& fwrite(&n, 4, 1, f) == 1
+		&& (n == 0 || fwrite(cell.data(), 4, n, f) == n)
+		&& (n == 0 || fwrite(en.data(), 4, n, f) == n)
+		&& fwrite(grass.data(), 2, grass.size(), f) == grass.size();
+	if (fclose(f) != 0) ok = false;
+	return ok ? PP_SUCCESS : PP_UNABLE_SAVE_STATS;
+}
+
+extern "C" int pp_sim_restore(const char *path, const pp_opts *opts, pp_sim **out)
+{
+	if (!path || !out) return PP_INVALID_ARGS;
+	*out = nullptr;
+	FILE *f = fopen(path, "rb");
+	if (!f) return PP_UNABLE_TO_OPEN_PARAMS_FILE;
+	char magic[8];
+	PPParameters p;
+	uint64_t seed = 0;
+	uint32_t iter = 0, n = 0;
+	bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, SNAP_MAGIC, 8) == 0
+		&& fread(&p, sizeof(p), 1, f) == 1 && fread(&seed, 8, 1, f) == 1
+		&& fread(&iter, 4, 1, f) == 1 && fread(&n, 4, 1, f) == 1
+		&& p.grid_x > 0 && p.grid_y > 0 && p.grid_x <= 65535 && p.grid_y <= 65535
+		&& n < 0x80000000u;
+	std::vector<uint32_t> cell, en;
+	std::vector<uint16_t> grass;
+	if (ok) {
+		cell.resize(std::max<uint32_t>(n, 1));
+		en.resize(std::max<uint32_t>(n, 1));
+		grass.resize((size_t) p.grid_x * p.grid_y);
+		ok = (n == 0 || fread(cell.data(), 4, n, f) == n)
+			&& (n == 0 || fread(en.data(), 4, n, f) == n)
+			&& fread(grass.data(), 2, grass.size(), f) == grass.size();
+	}
+	fclose(f);
+	if (!ok) return PP_INVALID_PARAMS_FILE;
+	RunSpec spec;
+	spec.init_cell = cell.data();
+	spec.init_val = en.data();
+	spec.init_grass = grass.data();
+	spec.init_n = n;
+	spec.start_iter = iter;
+	return sim_create(&p, seed, opts, &spec, out);
 }
 
 extern "C" int pp_sim_stats0(pp_sim *sim, PPStatistics *out)
@@ -937,7 +1081,7 @@ extern "C" int pp_sim_info(pp_sim *sim, uint32_t *iter, uint32_t *n_agents,
 	uint32_t *capacity)
 {
 	if (!sim) return PP_INVALID_ARGS;
-	if (iter) *iter = sim->world.giter();
+	if (iter) *iter = sim->iter0 + sim->world.giter();
 	if (n_agents) *n_agents = sim->world.n_agents_dev();
 	if (capacity) *capacity = sim->world.dev().cap;
 	return PP_SUCCESS;

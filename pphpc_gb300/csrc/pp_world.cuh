@@ -17,6 +17,17 @@ struct RunSpec {
 	PPParameters p;
 	uint64_t seed;
 	uint32_t iters;          /* UINT32_MAX = open-ended */
+	/* A run resumed from a snapshot (host arrays, run-local cells in
+	 * canonical order, grass countdowns) at iteration start_iter; null
+	 * init_val = a fresh run initialised from its seed. */
+	const uint32_t *init_cell = nullptr, *init_val = nullptr;
+	const uint16_t *init_grass = nullptr;
+	uint32_t init_n = 0;
+	uint32_t start_iter = 0;
+	uint64_t agents() const
+	{
+		return init_val ? (uint64_t) init_n : (uint64_t) p.init_sheep + p.init_wolves;
+	}
 };
 
 struct WorldConfig {
@@ -81,6 +92,8 @@ public:
 private:
 	int alloc(size_t bytes, void **p);
 	int sort_into(uint32_t n, uint32_t *dst_k, uint32_t *dst_v);
+	int load_run_state(const RunSpec &spec, const RunDev &run, uint32_t base,
+		PPStatistics *row0);
 	int build_graph();
 	int init_run_device(uint32_t r, uint32_t base, const RunSpec &spec);
 	cudaError_t enqueue_one(const cudaEvent_t *marks = nullptr);
