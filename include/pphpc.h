@@ -212,6 +212,19 @@ int pp_sim_snapshot_save(pp_sim *sim, const char *path);
  * the file is not a snapshot. */
 int pp_sim_restore(const char *path, const pp_opts *opts, pp_sim **out);
 
+/* The simulation's parameters (as checked at creation or restore). */
+int pp_sim_params(pp_sim *sim, PPParameters *out);
+
+/* Append the state after the last iteration to two text files in the line
+ * formats of pp_gpu's PPG_DUMP debugging mode (pp_gpu.c:415-555): agents
+ * (index, packed agent, position, type, energy) and cells (position, first
+ * and last agent index, grass countdown). dump_type as PPG_DUMP: 0x10
+ * keeps only cells holding agents. The initial state (iteration 0) is
+ * labelled -1, as the reference labels its dump before the first
+ * iteration. */
+int pp_sim_dump(pp_sim *sim, int dump_type, const char *agents_path,
+	const char *cells_path);
+
 int pp_sim_destroy(pp_sim *sim);
 
 /* ------------------------------------------------------------------ */

@@ -138,6 +138,8 @@ ABI = {
     "pp_sim_io_bytes": (C.c_int, [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)]),
     "pp_sim_destroy": (C.c_int, [C.c_void_p]),
     "pp_sim_snapshot_save": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "pp_sim_params": (C.c_int, [C.c_void_p, _P(PPParameters)]),
+    "pp_sim_dump": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_char_p]),
     "pp_sim_restore": (C.c_int, [C.c_char_p, _P(PPOpts), _P(C.c_void_p)]),
     "pp_philox_fill": (C.c_int, [C.c_uint32] * 7 + [_u32p]),
     "pp_move_host": (C.c_int, [_P(PPParameters), C.c_uint64, C.c_uint32, C.c_uint32,
@@ -251,6 +253,11 @@ class Simulation:
         `params` must be the saved simulation's parameters (the file holds
         them; they size the Python-side buffers)."""
         return cls(params, _restore=path, **kw)
+
+    def dump(self, agents_path, cells_path, dump_type=0x01):
+        """Append the state in the reference's PPG_DUMP formats (pp_sim_dump)."""
+        _check(lib().pp_sim_dump(self._h, dump_type, os.fsencode(agents_path),
+                                 os.fsencode(cells_path)), "pp_sim_dump")
 
     def save(self, path):
         """Write a snapshot of the current state (pp_sim_snapshot_save)."""

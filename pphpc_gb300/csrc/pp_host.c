@@ -16,6 +16,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <stdarg.h>
+#include <stdlib.h>
 
 #include "../../include/pphpc.h"
 
@@ -166,6 +167,99 @@ int pp_stats_save(const char *filename, const PPStatistics *stats,
 	}
 	if (fclose(fp) != 0) return PP_UNABLE_SAVE_STATS;
 	return PP_SUCCESS;
+}
+
+/* One iteration of the debugging dump of pp_gpu's PPG_DUMP mode
+ * (opencl/pp/pp_gpu.c:415-555), appended to two text files in its line
+ * formats:
+ *   agents: "\nIter %d, max_agents_iter=%d, ..." then, per agent k of the
+ *           canonical array, "[%4d] %016lx: (%4d, %4d) type=%d energy=%d"
+ *           with the reference's 64-bit packing x << 48 | y << 32 |
+ *           type << 16 | energy (16 low bits; no hash);
+ *   cells:  "\nIteration %d" then, per cell, "(x, y) -> (first, last) ...
+ *           [Grass: countdown]", first = last = the pool size for an empty
+ *           cell, or "(x, y) -> (-, -) [Grass: countdown]" for the initial
+ *           state (iteration -1).
+ * dump_type 0x10 keeps only cells holding agents (and 0x01, only live
+ * agents, changes nothing: the state holds live agents only). Indices are
+ * positions in the state after the iteration's actions. */
+int pp_sim_dump(pp_sim *sim, int dump_type, const char *agents_path,
+	const char *cells_path)
+{
+	if (!sim || !agents_path || !cells_path) return PP_INVALID_ARGS;
+	uint32_t it = 0, na = 0, cap = 0;
+	int rc = pp_sim_info(sim, &it, &na, &cap);
+	if (rc) return rc;
+	uint32_t n = 0;
+	rc = pp_sim_get_state(sim, NULL, NULL, 0, &n, NULL);
+	if (rc) return rc;
+	PPParameters p;
+	rc = pp_sim_params(sim, &p);
+	if (rc) return rc;
+	const uint32_t cells = p.grid_x * p.grid_y;
+	uint32_t *cell = (uint32_t *) malloc(sizeof(uint32_t) * (n ? n : 1));
+	uint32_t *en = (uint32_t *) malloc(sizeof(uint32_t) * (n ? n : 1));
+	uint16_t *grass = (uint16_t *) malloc(sizeof(uint16_t) * cells);
+	uint32_t *first = (uint32_t *) malloc(sizeof(uint32_t) * cells);
+	uint32_t *last = (uint32_t *) malloc(sizeof(uint32_t) * cells);
+	FILE *fa = NULL, *fc = NULL;
+	if (!cell || !en || !grass || !first || !last) {
+		rc = PP_OUT_OF_RESOURCES;
+		goto done;
+	}
+	rc = pp_sim_get_state(sim, cell, en, n, &n, grass);
+	if (rc) goto done;
+	fa = fopen(agents_path, "a");
+	fc = fopen(cells_path, "a");
+	if (!fa || !fc) {
+		rc = PP_UNABLE_SAVE_STATS;
+		goto done;
+	}
+	const int iter = it == 0 ? -1 : (int) it;
+	fprintf(fa, "\nIter %d, max_agents_iter=%u, gws_reduce_agent1=%u, "
+		"gws_action_ag=%u, gws_mov_ag=%u\n", iter, cap, n, n, n);
+	for (uint32_t k = 0; k < n; k++) {
+		const uint32_t x = cell[k] % p.grid_x, y = cell[k] / p.grid_x;
+		const uint32_t type = en[k] >> 31, e = en[k] & 0x7fffffffu;
+		const unsigned long long ag = ((unsigned long long) x << 48)
+			| ((unsigned long long) y << 32) | ((unsigned long long) type << 16)
+			| (e & 0xffffu);
+		fprintf(fa, "[%4u] %016llx: (%4u, %4u) type=%u energy=%u\n",
+			k, ag, x, y, type, e);
+	}
+	for (uint32_t c = 0; c < cells; c++) first[c] = last[c] = cap;
+	for (uint32_t k = 0; k < n; k++) {
+		if (first[cell[k]] == cap) first[cell[k]] = k;
+		last[cell[k]] = k;
+	}
+	fprintf(fc, "\nIteration %d\n", iter);
+	int blank_line = 0;
+	for (uint32_t c = 0; c < cells; c++) {
+		if (!(dump_type & 0x10) || (iter != -1 && first[c] != cap)) {
+			if (blank_line) fprintf(fc, "\n");
+			blank_line = 0;
+			if (iter != -1)
+				fprintf(fc, "(%u, %u) -> (%u, %u) %s [Grass: %u]\n",
+					c % p.grid_x, c / p.grid_x, first[c], last[c],
+					first[c] != last[c] ? "More than 1 agent present" : "",
+					(unsigned) grass[c]);
+			else
+				fprintf(fc, "(%u, %u) -> (-, -) [Grass: %u]\n",
+					c % p.grid_x, c / p.grid_x, (unsigned) grass[c]);
+		} else {
+			blank_line = 1;
+		}
+	}
+	if (ferror(fa) || ferror(fc)) rc = PP_UNABLE_SAVE_STATS;
+done:
+	if (fa && fclose(fa) != 0) rc = PP_UNABLE_SAVE_STATS;
+	if (fc && fclose(fc) != 0) rc = PP_UNABLE_SAVE_STATS;
+	free(cell);
+	free(en);
+	free(grass);
+	free(first);
+	free(last);
+	return rc;
 }
 
 const char *pp_version(void)

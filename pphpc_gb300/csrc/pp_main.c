@@ -4,13 +4,16 @@
  *
  *   pp_gb300 [-p PARAMS] [-s STATS] [-r SEED] [-d DEVICE] [-m MAX_AGENTS]
  *            [--iters N] [-i PROF_FILE] [-t TILE] [--digit-bits B]
- *            [--no-graph]
+ *            [--no-graph] [--dump TYPE]
  *
  * -p/-s/-r/-d/-m keep the reference's meaning and defaults (config.txt,
  * stats.txt, seed 0, device 0, agent pool); --iters overrides ITERS from
  * the parameters file (the reference has no such knob: -i there is the
- * profiling export, kept here as a two-column kernel-time file). The
- * exit status is a pp_error_codes value, as in the reference.
+ * profiling export, kept here as a two-column kernel-time file). --dump
+ * writes dump_agents.txt and dump_cells.txt after every iteration in the
+ * formats of the reference's compile-time PPG_DUMP mode (pp_gpu.c:28-47,
+ * 415-555), TYPE as there (0x00, 0x01, 0x10, 0x11). The exit status is a
+ * pp_error_codes value, as in the reference.
  */
 #include <getopt.h>
 #include <stdio.h>
@@ -31,7 +34,8 @@ static void usage(const char *argv0)
 {
 	fprintf(stderr,
 		"Usage: %s [-p FILE] [-s FILE] [-r SEED] [-d INDEX] [-m MAX]\n"
-		"          [--iters N] [-i FILE] [-t TILE] [--digit-bits B] [--no-graph]\n",
+		"          [--iters N] [-i FILE] [-t TILE] [--digit-bits B] [--no-graph]\n"
+		"          [--dump TYPE]\n",
 		argv0);
 }
 
@@ -40,6 +44,7 @@ int main(int argc, char **argv)
 	const char *params_file = NULL, *stats_file = NULL, *prof_file = NULL;
 	long long seed = 0;
 	long long iters_override = -1;
+	int dump_type = -1;
 	pp_opts opts;
 	pp_opts_default(&opts);
 	static struct option longopts[] = {
@@ -53,6 +58,7 @@ int main(int argc, char **argv)
 		{"tile", required_argument, 0, 't'},
 		{"digit-bits", required_argument, 0, 'D'},
 		{"no-graph", no_argument, 0, 'G'},
+		{"dump", required_argument, 0, 'U'},
 		{"help", no_argument, 0, 'h'},
 		{0, 0, 0, 0}
 	};
@@ -69,6 +75,7 @@ int main(int argc, char **argv)
 		case 't': opts.tile_cells = (uint32_t) strtoul(optarg, NULL, 0); break;
 		case 'D': opts.sort_digit_bits = (uint32_t) strtoul(optarg, NULL, 0); break;
 		case 'G': opts.use_graph = 0; break;
+		case 'U': dump_type = (int) strtol(optarg, NULL, 0); break;
 		case 'h': usage(argv[0]); return PP_SUCCESS;
 		default: usage(argv[0]); return PP_UNKNOWN_ARGS;
 		}
@@ -103,7 +110,20 @@ int main(int argc, char **argv)
 	}
 	pp_sim_stats0(sim, &rows[0]);
 	double t1 = now_s();
-	rc = pp_sim_step(sim, params.iters, rows + 1);
+	if (dump_type >= 0) {
+		/* debugging mode: one iteration at a time, dumped after each */
+		const char *fa = "dump_agents.txt", *fc = "dump_cells.txt";
+		FILE *f1 = fopen(fa, "w"), *f2 = fopen(fc, "w");
+		if (f1) fclose(f1);
+		if (f2) fclose(f2);
+		rc = (f1 && f2) ? pp_sim_dump(sim, dump_type, fa, fc) : PP_UNABLE_SAVE_STATS;
+		for (uint32_t i = 0; i < params.iters && rc == PP_SUCCESS; i++) {
+			rc = pp_sim_step(sim, 1, rows + 1 + i);
+			if (rc == PP_SUCCESS) rc = pp_sim_dump(sim, dump_type, fa, fc);
+		}
+	} else {
+		rc = pp_sim_step(sim, params.iters, rows + 1);
+	}
 	double t2 = now_s();
 	if (rc == PP_OUT_OF_RESOURCES)
 		fprintf(stderr, "Error: agents required above the pool limit "

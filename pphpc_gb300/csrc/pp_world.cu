@@ -1015,6 +1015,13 @@ extern "C" int pp_sim_restore(const char *path, const pp_opts *opts, pp_sim **ou
 	return sim_create(&p, seed, opts, &spec, out);
 }
 
+extern "C" int pp_sim_params(pp_sim *sim, PPParameters *out)
+{
+	if (!sim || !out) return PP_INVALID_ARGS;
+	*out = sim->params;
+	return PP_SUCCESS;
+}
+
 extern "C" int pp_sim_stats0(pp_sim *sim, PPStatistics *out)
 {
 	if (!sim || !out) return PP_INVALID_ARGS;
