@@ -125,7 +125,25 @@ typedef struct pp_opts {
 	uint32_t autotune;      /* 1 = when tile_cells is 0, measure the candidate
 	                           geometries (pp_autotune) and use the fastest;
 	                           0 = built-in choice */
+	uint32_t ss_from;       /* focal measures: the steady state is the
+	                           iterations after ss_from (default 1000) */
 } pp_opts;
+
+/* PPHPC focal measures of a run's six outputs, in the order sheep, wolves,
+ * live grass, mean sheep energy, mean wolf energy, mean grass countdown
+ * (the columns of the stats file): the maximum and minimum over iterations
+ * 0..t with the first iteration reaching each, and the mean and sample
+ * standard deviation over the steady state (iterations after ss_from).
+ * Computed on the GPU as the iterations run, so a caller needs no stats
+ * rows to get them. No counterpart in the reference (the measures are
+ * those of Fachada et al., "Towards a standard model for research in
+ * agent-based modeling and simulation", PeerJ CS 2015). */
+typedef struct pp_focal {
+	double max[6], min[6], ss_mean[6], ss_std[6];
+	uint32_t argmax[6], argmin[6];
+	uint32_t ss_n;          /* steady-state iterations counted */
+	uint32_t pad;
+} pp_focal;
 
 /* Fill `opts` with defaults. */
 void pp_opts_default(pp_opts *opts);
@@ -214,6 +232,10 @@ int pp_sim_restore(const char *path, const pp_opts *opts, pp_sim **out);
 
 /* The simulation's parameters (as checked at creation or restore). */
 int pp_sim_params(pp_sim *sim, PPParameters *out);
+
+/* The focal measures of the iterations run so far (from iteration 0, or
+ * the restored iteration). */
+int pp_sim_focal(pp_sim *sim, pp_focal *out);
 
 /* Append the state after the last iteration to two text files in the line
  * formats of pp_gpu's PPG_DUMP debugging mode (pp_gpu.c:415-555): agents
@@ -321,6 +343,7 @@ typedef struct pp_serve_opts {
 	uint32_t max_runs;          /* resident-run slots                     */
 	uint32_t pool_factor;       /* agent slots per run = factor x initial */
 	uint32_t stats_chunk;       /* iterations between stats streaming     */
+	uint32_t ss_from;           /* focal measures' steady state: t > ss_from */
 } pp_serve_opts;
 
 void pp_serve_opts_default(pp_serve_opts *opts);
@@ -355,6 +378,10 @@ int pp_serve_status(pp_server *srv, uint64_t id, pp_serve_event *ev);
 
 /* Number of queued and resident runs. */
 int pp_serve_load(pp_server *srv, uint32_t *queued, uint32_t *resident);
+
+/* The focal measures of a finished request (PP_INVALID_ARGS until it has
+ * finished successfully). */
+int pp_serve_focal(pp_server *srv, uint64_t id, pp_focal *out);
 
 /* Release a finished request's stats. */
 int pp_serve_release(pp_server *srv, uint64_t id);

@@ -75,7 +75,7 @@ class PPOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("max_agents", C.c_uint32),
                 ("tile_cells", C.c_uint32), ("sort_digit_bits", C.c_uint32),
                 ("use_graph", C.c_uint32), ("sort_pipeline", C.c_uint32),
-                ("autotune", C.c_uint32)]
+                ("autotune", C.c_uint32), ("ss_from", C.c_uint32)]
 
 
 class PPRunDesc(C.Structure):
@@ -92,7 +92,7 @@ class PPBatchOpts(C.Structure):
 class PPServeOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("mem_budget_bytes", C.c_uint64),
                 ("max_runs", C.c_uint32), ("pool_factor", C.c_uint32),
-                ("stats_chunk", C.c_uint32)]
+                ("stats_chunk", C.c_uint32), ("ss_from", C.c_uint32)]
 
 
 class PPServeEvent(C.Structure):
@@ -103,6 +103,20 @@ class PPServeEvent(C.Structure):
 class PPTuning(C.Structure):
     _fields_ = [("tile_cells", C.c_uint32), ("sort_pipeline", C.c_uint32),
                 ("sort_digit_bits", C.c_uint32), ("ns_per_agent_step", C.c_float)]
+
+
+class PPFocal(C.Structure):
+    _fields_ = [("max", C.c_double * 6), ("min", C.c_double * 6),
+                ("ss_mean", C.c_double * 6), ("ss_std", C.c_double * 6),
+                ("argmax", C.c_uint32 * 6), ("argmin", C.c_uint32 * 6),
+                ("ss_n", C.c_uint32), ("pad", C.c_uint32)]
+
+    def as_array(self):
+        """(6 outputs, 6 measures): max, argmax, min, argmin, ss_mean,
+        ss_std -- the layout of tests/focal.py."""
+        import numpy as np
+        return np.array([[self.max[k], self.argmax[k], self.min[k], self.argmin[k],
+                          self.ss_mean[k], self.ss_std[k]] for k in range(6)])
 
 
 class KernelProf(C.Structure):
@@ -139,6 +153,8 @@ ABI = {
     "pp_sim_destroy": (C.c_int, [C.c_void_p]),
     "pp_sim_snapshot_save": (C.c_int, [C.c_void_p, C.c_char_p]),
     "pp_sim_params": (C.c_int, [C.c_void_p, _P(PPParameters)]),
+    "pp_sim_focal": (C.c_int, [C.c_void_p, _P(PPFocal)]),
+    "pp_serve_focal": (C.c_int, [C.c_void_p, C.c_uint64, _P(PPFocal)]),
     "pp_sim_dump": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_char_p]),
     "pp_sim_restore": (C.c_int, [C.c_char_p, _P(PPOpts), _P(C.c_void_p)]),
     "pp_philox_fill": (C.c_int, [C.c_uint32] * 7 + [_u32p]),
@@ -227,7 +243,7 @@ class Simulation:
 
     def __init__(self, params, seed=0, device=0, max_agents=0, tile_cells=0,
                  digit_bits=0, use_graph=True, sort_pipeline=False, autotune=False,
-                 _restore=None):
+                 ss_from=1000, _restore=None):
         L = lib()
         o = PPOpts()
         L.pp_opts_default(C.byref(o))
@@ -238,6 +254,7 @@ class Simulation:
         o.use_graph = 1 if use_graph else 0
         o.sort_pipeline = 1 if sort_pipeline else 0
         o.autotune = 1 if autotune else 0
+        o.ss_from = ss_from
         self.params = params
         self._h = C.c_void_p()
         if _restore is not None:
@@ -253,6 +270,12 @@ class Simulation:
         `params` must be the saved simulation's parameters (the file holds
         them; they size the Python-side buffers)."""
         return cls(params, _restore=path, **kw)
+
+    def focal(self):
+        """PPHPC focal measures computed on the GPU (pp_sim_focal)."""
+        f = PPFocal()
+        _check(lib().pp_sim_focal(self._h, C.byref(f)), "pp_sim_focal")
+        return f
 
     def dump(self, agents_path, cells_path, dump_type=0x01):
         """Append the state in the reference's PPG_DUMP formats (pp_sim_dump)."""
@@ -381,7 +404,7 @@ class Server:
     """Continuous-batching server (pp_serve_* of the C ABI)."""
 
     def __init__(self, mem_budget_bytes=8 << 30, max_runs=256, pool_factor=4,
-                 stats_chunk=64, device=0):
+                 stats_chunk=64, device=0, ss_from=1000):
         L = lib()
         o = PPServeOpts()
         L.pp_serve_opts_default(C.byref(o))
@@ -390,6 +413,7 @@ class Server:
         o.max_runs = max_runs
         o.pool_factor = pool_factor
         o.stats_chunk = stats_chunk
+        o.ss_from = ss_from
         self._h = C.c_void_p()
         _check(L.pp_serve_create(C.byref(o), C.byref(self._h)), "pp_serve_create")
 
@@ -425,6 +449,12 @@ class Server:
         _check(lib().pp_serve_read(self._h, rid, first, n, rows, C.byref(got)),
                "pp_serve_read")
         return list(rows)[:got.value]
+
+    def focal(self, rid):
+        """Focal measures of a finished request (pp_serve_focal)."""
+        f = PPFocal()
+        _check(lib().pp_serve_focal(self._h, rid, C.byref(f)), "pp_serve_focal")
+        return f
 
     def release(self, rid):
         _check(lib().pp_serve_release(self._h, rid), "pp_serve_release")

@@ -149,8 +149,57 @@ struct RunDev {
 	uint32_t start_giter;      /* world iteration at which iter 1 runs - 1 */
 	uint32_t active;           /* 0 = finished or empty slot               */
 	uint32_t fbase;            /* this run's regrowth histogram (restart+1 slots) */
+	uint32_t ss_from;          /* focal measures: steady state is t > ss_from */
 	fastdiv gxdiv;
 };
+
+/* Running PPHPC focal measures of one run over its six outputs (sheep,
+ * wolves, live grass, mean sheep energy, mean wolf energy, mean grass
+ * countdown): max and min with the first iteration reaching them, and the
+ * steady-state sum and sum of squares. */
+struct FocalDev {
+	double mx[6], mn[6], sum[6], sq[6];
+	uint32_t amx[6], amn[6];
+	uint32_t n, pad;
+};
+
+__host__ __device__ __forceinline__ void focal_outputs(uint32_t sheep,
+	uint32_t wolves, uint32_t grass, uint64_t sheep_en, uint64_t wolves_en,
+	uint64_t grass_en, uint32_t ncells, double o[6])
+{
+	o[0] = sheep;
+	o[1] = wolves;
+	o[2] = grass;
+	o[3] = sheep ? (double) sheep_en / (double) sheep : 0.0;
+	o[4] = wolves ? (double) wolves_en / (double) wolves : 0.0;
+	o[5] = (double) grass_en / (double) ncells;
+}
+
+/* Fold the outputs of iteration t into f (t == first: start afresh). */
+__host__ __device__ __forceinline__ void focal_fold(FocalDev &f, const double o[6],
+	uint32_t t, bool first, uint32_t ss_from)
+{
+	if (first) {
+		for (int k = 0; k < 6; k++) {
+			f.mx[k] = f.mn[k] = o[k];
+			f.amx[k] = f.amn[k] = t;
+			f.sum[k] = f.sq[k] = 0.0;
+		}
+		f.n = 0;
+	} else {
+		for (int k = 0; k < 6; k++) {
+			if (o[k] > f.mx[k]) { f.mx[k] = o[k]; f.amx[k] = t; }
+			if (o[k] < f.mn[k]) { f.mn[k] = o[k]; f.amn[k] = t; }
+		}
+	}
+	if (t > ss_from) {
+		for (int k = 0; k < 6; k++) {
+			f.sum[k] += o[k];
+			f.sq[k] += o[k] * o[k];
+		}
+		f.n++;
+	}
+}
 
 /* Per-world counters in device memory. The finish kernel's last CTA
  * advances the iteration and resets the per-launch counters for the next

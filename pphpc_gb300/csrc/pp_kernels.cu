@@ -600,6 +600,20 @@ __global__ void __launch_bounds__(256) k_finish(WorldDev w)
 	}
 	__syncthreads();
 	if (FULL && s_last) {
+		/* every run's row g is complete: fold it into its focal measures
+		 * (read through L2: the row was summed by atomics) */
+		for (uint32_t r = threadIdx.x; r < w.nruns_cap; r += blockDim.x) {
+			const RunDev &run = w.runs[r];
+			const uint32_t t = g - run.start_giter;
+			if (!run_live(run, t)) continue;
+			const PPStatistics *st = &w.ring[(size_t) (g % w.ring_rows) * w.nruns_cap + r];
+			double o[6];
+			focal_outputs(__ldcg(&st->sheep), __ldcg(&st->wolves), __ldcg(&st->grass),
+				__ldcg((const unsigned long long *) &st->sheep_en),
+				__ldcg((const unsigned long long *) &st->wolves_en),
+				__ldcg((const unsigned long long *) &st->grass_en), run.ncells, o);
+			focal_fold(w.focal[r], o, t, false, run.ss_from);
+		}
 		for (uint32_t q = threadIdx.x; q < 8 * 256; q += blockDim.x) w.hist[q] = 0;
 		const uint32_t nrow = (g + 1) % w.ring_rows;
 		uint32_t *rowp = reinterpret_cast<uint32_t *>(
@@ -607,6 +621,15 @@ __global__ void __launch_bounds__(256) k_finish(WorldDev w)
 		const uint32_t words = w.nruns_cap * (sizeof(PPStatistics) / 4);
 		for (uint32_t q = threadIdx.x; q < words; q += blockDim.x) rowp[q] = 0;
 	}
+}
+
+__global__ void k_focal_init(WorldDev w, uint32_t r, uint32_t row, uint32_t t0)
+{
+	const PPStatistics *st = &w.ring[(size_t) row * w.nruns_cap + r];
+	double o[6];
+	focal_outputs(st->sheep, st->wolves, st->grass, st->sheep_en, st->wolves_en,
+		st->grass_en, w.runs[r].ncells, o);
+	focal_fold(w.focal[r], o, t0, true, w.runs[r].ss_from);
 }
 
 /* Regions of tiles [first, first + count) from the tile offsets of a
@@ -804,6 +827,13 @@ cudaError_t set_act_smem_limits(size_t bytes)
 	e = cudaFuncSetAttribute(k_act<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
 	if (e != cudaSuccess) return e;
 	return cudaFuncSetAttribute(k_act<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+}
+
+cudaError_t enqueue_focal_init(const WorldDev &w, uint32_t r, uint32_t row,
+	uint32_t t0, cudaStream_t s)
+{
+	k_focal_init<<<1, 1, 0, s>>>(w, r, row, t0);
+	return cudaGetLastError();
 }
 
 cudaError_t enqueue_init_grass(const WorldDev &w, const RunDev &run,

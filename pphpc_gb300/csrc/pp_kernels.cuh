@@ -47,6 +47,7 @@ struct WorldDev {
 	                           runs' first moves from 2 * cap on */
 	uint2 *inbox;             /* [2][n_tiles][IBX]                          */
 	uint32_t *inbox_n;        /* [2][n_tiles]                               */
+	FocalDev *focal;          /* [nruns_cap] running focal measures         */
 	uint32_t fused;
 };
 
@@ -85,6 +86,11 @@ cudaError_t enqueue_fused_bases(const WorldDev &w, const LaunchCfg &lc,
 	cudaStream_t s);
 
 cudaError_t set_step_smem_limits(size_t bytes);
+
+/* Focal measures of run r restarted from its stats row `row` (its
+ * iteration t0). */
+cudaError_t enqueue_focal_init(const WorldDev &w, uint32_t r, uint32_t row,
+	uint32_t t0, cudaStream_t s);
 
 /* Initialisation of a run: grass of its tiles; its initial agents in
  * creation order into k/v[base ..) (sorted by cell afterwards); the stats

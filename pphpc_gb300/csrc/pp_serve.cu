@@ -34,6 +34,8 @@ struct Request {
 	uint32_t n_rows = 0;          /* rows available */
 	uint64_t reserve = 0;
 	std::vector<PPStatistics> rows;
+	bool has_focal = false;
+	pp_focal focal;
 };
 
 uint64_t reservation(const RunSpec &s, uint32_t pool_factor)
@@ -67,6 +69,7 @@ extern "C" void pp_serve_opts_default(pp_serve_opts *o)
 	o->max_runs = 256;
 	o->pool_factor = 4;
 	o->stats_chunk = 64;
+	o->ss_from = 1000;
 }
 
 extern "C" int pp_serve_create(const pp_serve_opts *opts, pp_server **out)
@@ -134,6 +137,7 @@ extern "C" int pp_serve_submit(pp_server *srv, const pp_run_desc *run,
 	rq.spec.p = p;
 	rq.spec.seed = run->seed;
 	rq.spec.iters = p.iters;
+	rq.spec.ss_from = srv->opts.ss_from;
 	rq.reserve = reservation(rq.spec, srv->opts.pool_factor ? srv->opts.pool_factor : 4);
 	uint64_t tiles_needed = ((uint64_t) p.grid_xy + 1023) / 1024;
 	if (rq.reserve > srv->cap || tiles_needed > srv->max_tiles)
@@ -149,6 +153,14 @@ extern "C" int pp_serve_submit(pp_server *srv, const pp_run_desc *run,
 static int finish_request(pp_server *srv, Request &rq, int status)
 {
 	int rc = PP_SUCCESS;
+	if (rq.resident && status == PP_SUCCESS) {
+		FocalDev f;
+		rc = srv->world.read_focal(rq.slot, &f);
+		if (rc == PP_SUCCESS) {
+			focal_export(f, &rq.focal);
+			rq.has_focal = true;
+		}
+	}
 	if (rq.resident) {
 		rc = srv->world.retire(rq.slot);
 		srv->slot_req[rq.slot] = 0;
@@ -245,6 +257,15 @@ extern "C" int pp_serve_read(pp_server *srv, uint64_t id, uint32_t first,
 	uint32_t m = std::min(avail, n);
 	if (m && rows) memcpy(rows, rq.rows.data() + first, (size_t) m * sizeof(PPStatistics));
 	if (n_out) *n_out = m;
+	return PP_SUCCESS;
+}
+
+extern "C" int pp_serve_focal(pp_server *srv, uint64_t id, pp_focal *out)
+{
+	if (!srv || !out) return PP_INVALID_ARGS;
+	auto it = srv->reqs.find(id);
+	if (it == srv->reqs.end() || !it->second.has_focal) return PP_INVALID_ARGS;
+	*out = it->second.focal;
 	return PP_SUCCESS;
 }
 

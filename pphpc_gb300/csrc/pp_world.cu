@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <cmath>
 #include <new>
 
 #include "pp_world.cuh"
@@ -107,6 +108,7 @@ static RunDev make_run(const RunSpec &s, uint32_t first_tile,
 	r.start_giter = start_giter;
 	r.active = 1;
 	r.fbase = fbase;
+	r.ss_from = s.ss_from;
 	r.gxdiv = fastdiv_make(s.p.grid_x);
 	return r;
 }
@@ -214,6 +216,7 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	PP_AL(w_.tile_run, (size_t) tiles * 2);
 	PP_AL(w_.runs, (size_t) nruns_cap * sizeof(RunDev));
 	PP_AL(w_.part, (size_t) tiles * 8 * sizeof(uint64_t));
+	PP_AL(w_.focal, (size_t) nruns_cap * sizeof(FocalDev));
 	size_t sort_tiles = ceil_div(cap, SORT_TILE) + 1;
 	PP_AL(w_.lb_sort, sort_tiles * 256 * sizeof(uint64_t));
 	PP_AL(w_.lb_fin, ((size_t) tiles + 1) * sizeof(uint64_t));
@@ -322,6 +325,10 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 		}
 		rc = cuda_status(enqueue_stats_run(w_, runs_h_[r], (uint32_t) r,
 			sorted_v + base_h[r], runs[r].p.init_sheep + runs[r].p.init_wolves, 0, s_));
+		if (rc) return rc;
+	}
+	for (size_t r = 0; r < runs.size(); r++) {
+		rc = cuda_status(enqueue_focal_init(w_, (uint32_t) r, 0, runs[r].start_iter, s_));
 		if (rc) return rc;
 	}
 	giter_ = 0;
@@ -789,6 +796,8 @@ int World::admit(const RunSpec &spec, uint32_t *slot_out)
 		rc = cuda_status(enqueue_stats_run(w_, run, slot, w_.vA, n0, row, s_));
 		if (rc) return rc;
 		PP_CK(cudaStreamSynchronize(s_));
+		rc = cuda_status(enqueue_focal_init(w_, slot, row, 0, s_));
+		if (rc) return rc;
 	} else {
 		/* The agents go to the admission area of the region buffer (after
 		 * the 2 * cap slots the act writes), as the regions of the run's
@@ -801,10 +810,21 @@ int World::admit(const RunSpec &spec, uint32_t *slot_out)
 		adm_used_ += n0;
 		rc = cuda_status(enqueue_stats_run(w_, run, slot, w_.vR + adm, n0, row, s_));
 		if (rc) return rc;
+		rc = cuda_status(enqueue_focal_init(w_, slot, row, 0, s_));
+		if (rc) return rc;
 	}
 	h2d_ += sizeof(RunDev) + need * 2;
 	d2h_ += 4;
 	*slot_out = slot;
+	return PP_SUCCESS;
+}
+
+int World::read_focal(uint32_t r, FocalDev *out)
+{
+	PP_CK(cudaSetDevice(device_));
+	PP_CK(cudaStreamSynchronize(s_));
+	PP_CK(cudaMemcpy(out, &w_.focal[r], sizeof(FocalDev), cudaMemcpyDeviceToHost));
+	d2h_ += sizeof(FocalDev);
 	return PP_SUCCESS;
 }
 
@@ -880,6 +900,7 @@ extern "C" void pp_opts_default(pp_opts *o)
 	o->sort_digit_bits = 0;
 	o->use_graph = 1;
 	o->sort_pipeline = 0;
+	o->ss_from = 1000;
 }
 
 /* A simulation from parameters and a seed, or from a saved state (spec0's
@@ -927,6 +948,7 @@ static int sim_create(const PPParameters *params, uint64_t seed,
 	runs[0].p = p;
 	runs[0].seed = seed;
 	runs[0].iters = 0xffffffffu;
+	runs[0].ss_from = o.ss_from;
 	sim->iter0 = spec0 ? spec0->start_iter : 0;
 	rc = sim->world.create(runs, cfg);
 	if (rc == PP_SUCCESS) rc = sim->world.read_rows(0, 0, 0, &sim->stats0);
@@ -1013,6 +1035,33 @@ extern "C" int pp_sim_restore(const char *path, const pp_opts *opts, pp_sim **ou
 	spec.init_n = n;
 	spec.start_iter = iter;
 	return sim_create(&p, seed, opts, &spec, out);
+}
+
+void pp::focal_export(const FocalDev &f, pp_focal *out)
+{
+	memset(out, 0, sizeof(*out));
+	for (int k = 0; k < 6; k++) {
+		out->max[k] = f.mx[k];
+		out->min[k] = f.mn[k];
+		out->argmax[k] = f.amx[k];
+		out->argmin[k] = f.amn[k];
+		if (f.n) out->ss_mean[k] = f.sum[k] / f.n;
+		if (f.n > 1) {
+			const double var = (f.sq[k] - f.sum[k] * f.sum[k] / f.n) / (f.n - 1);
+			out->ss_std[k] = var > 0 ? sqrt(var) : 0.0;
+		}
+	}
+	out->ss_n = f.n;
+}
+
+extern "C" int pp_sim_focal(pp_sim *sim, pp_focal *out)
+{
+	if (!sim || !out) return PP_INVALID_ARGS;
+	FocalDev f;
+	int rc = sim->world.read_focal(0, &f);
+	if (rc) return rc;
+	focal_export(f, out);
+	return PP_SUCCESS;
 }
 
 extern "C" int pp_sim_params(pp_sim *sim, PPParameters *out)

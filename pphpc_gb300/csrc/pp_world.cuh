@@ -24,6 +24,7 @@ struct RunSpec {
 	const uint16_t *init_grass = nullptr;
 	uint32_t init_n = 0;
 	uint32_t start_iter = 0;
+	uint32_t ss_from = 1000;  /* focal measures: steady state is t > ss_from */
 	uint64_t agents() const
 	{
 		return init_val ? (uint64_t) init_n : (uint64_t) p.init_sheep + p.init_wolves;
@@ -66,6 +67,8 @@ public:
 	/* Admission of a run into a free slot and tile range (serving). */
 	int admit(const RunSpec &spec, uint32_t *slot_out);
 	int retire(uint32_t slot);
+	/* The running focal measures of run slot r (synchronises). */
+	int read_focal(uint32_t r, FocalDev *out);
 	bool fits(const RunSpec &spec) const;
 
 	uint32_t giter() const { return giter_; }
@@ -133,6 +136,9 @@ public:
 private:
 	std::vector<uint32_t> reserve_of_;
 };
+
+/* Mean and standard deviation from the running sums (C ABI form). */
+void focal_export(const FocalDev &f, pp_focal *out);
 
 /* Pick tile size and digit width for a world. */
 void choose_geometry(uint32_t total_cells, uint32_t cap, WorldConfig &cfg);
