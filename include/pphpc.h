@@ -127,6 +127,11 @@ typedef struct pp_opts {
 	                           0 = built-in choice */
 	uint32_t ss_from;       /* focal measures: the steady state is the
 	                           iterations after ss_from (default 1000) */
+	uint32_t agent_size;    /* the reference's -a/--agent-size (pp_gpu.c:334,
+	                           1632-1634): 64 = energy modulo 2^16 as in its
+	                           64-bit agents, 32 = modulo 2^11 as in its
+	                           32-bit agents (grids up to 1024 x 1024);
+	                           0 = modulo 2^30 (default); else PP_INVALID_ARGS */
 } pp_opts;
 
 /* PPHPC focal measures of a run's six outputs, in the order sheep, wolves,
@@ -321,6 +326,7 @@ typedef struct pp_batch_opts {
 	uint32_t stats_chunk;   /* iterations between stats copies to the host */
 	uint32_t autotune;      /* 1 = when tile_cells is 0, tune on the largest
 	                           run's parameters at the batch's pool density */
+	uint32_t agent_size;    /* energy field of every run, as pp_opts.agent_size */
 } pp_batch_opts;
 
 void pp_batch_opts_default(pp_batch_opts *opts);
@@ -344,6 +350,7 @@ typedef struct pp_serve_opts {
 	uint32_t pool_factor;       /* agent slots per run = factor x initial */
 	uint32_t stats_chunk;       /* iterations between stats streaming     */
 	uint32_t ss_from;           /* focal measures' steady state: t > ss_from */
+	uint32_t agent_size;        /* energy field of every run, as pp_opts.agent_size */
 } pp_serve_opts;
 
 void pp_serve_opts_default(pp_serve_opts *opts);

@@ -14,8 +14,9 @@
  * gives the same results.
  *
  * Canonical step (iteration t = 1..iters):
- *   1. move   -- agent of rank k in cell c: energy <= 1 -> dies; else
- *               energy -= 1 and one of 5 directions (stay, x+1, x-1, y+1,
+ *   1. move   -- agent of rank k in cell c: energy := energy - 1 modulo
+ *               2^energy_bits; 0 -> dies (pp_gpu.cl:805-810); else
+ *               one of 5 directions (stay, x+1, x-1, y+1,
  *               y-1, per-row toroidal wrap as in pp_gpu.cl:771-800) drawn
  *               from Philox(ctr={c, t, MOVE, k}).w0.
  *   2. grass  -- countdown > 0 -> countdown - 1 (pp_gpu.cl:465).
@@ -28,7 +29,8 @@
  *               a wolf eats the first not-yet-eaten sheep of the cell
  *               (eaten sheep may have acted already); a sheep that is not
  *               yet eaten at its turn eats the grass if countdown == 0
- *               (countdown := restart, energy += gain); every agent that
+ *               (countdown := restart, energy += gain; every energy
+ *               gain is modulo 2^energy_bits); every agent that
  *               acts then reproduces if energy > threshold and
  *               draw(Philox({c, t, ACT, k}).w1, 100) < prob: the child
  *               gets energy/2 and the parent keeps the rest. Newborns
@@ -98,6 +100,12 @@ struct ppo_state {
 };
 
 static uint32_t energy_of(uint32_t en) { return en & PPO_ENERGY_MASK; }
+
+uint32_t ppo_energy_mask(const ppo_params *p)
+{
+	uint32_t b = p->energy_bits ? p->energy_bits : 30;
+	return b >= 30 ? 0x3fffffffu : (1u << b) - 1;
+}
 static uint32_t type_of(uint32_t en) { return en >> 31; }
 
 ppo_state *ppo_create(const ppo_params *p, uint64_t seed, uint32_t capacity)
@@ -145,7 +153,7 @@ ppo_state *ppo_create(const ppo_params *p, uint64_t seed, uint32_t capacity)
 		uint32_t y = ppo_draw(r[1], p->grid_y);
 		uint32_t wolf = a >= p->init_sheep;
 		uint32_t gain = wolf ? p->wolves_gain : p->sheep_gain;
-		uint32_t e = 1 + ppo_draw(r[2], 2 * gain);
+		uint32_t e = (1 + ppo_draw(r[2], 2 * gain)) & ppo_energy_mask(p);
 		s->cell2[a] = y * p->grid_x + x;
 		s->en2[a] = (wolf ? PPO_TYPE_BIT : 0) | e;
 	}
@@ -187,6 +195,7 @@ void ppo_move(const ppo_params *p, uint64_t seed, uint32_t iter, uint32_t n,
 	uint32_t *cell_out, uint32_t *en_out)
 {
 	uint32_t GX = p->grid_x, GY = p->grid_y, C = p->grid_x * p->grid_y;
+	uint32_t emask = ppo_energy_mask(p);
 	/* rank[c] = agents of cell c seen so far: an agent's rank is its
 	 * position in its cell's list (earlier array entries of that cell). */
 	uint32_t *rank = calloc((size_t) C + 1, sizeof(uint32_t));
@@ -194,7 +203,8 @@ void ppo_move(const ppo_params *p, uint64_t seed, uint32_t iter, uint32_t n,
 		uint32_t en = en_in[i];
 		uint32_t e = energy_of(en);
 		uint32_t k = cell_in[i] < C ? rank[cell_in[i]]++ : 0;
-		if (e <= 1) {
+		uint32_t e1 = (e - 1) & emask;
+		if (e1 == 0) {
 			cell_out[i] = C;           /* dead: sorts after every cell */
 			en_out[i] = en & PPO_TYPE_BIT;
 			continue;
@@ -211,7 +221,7 @@ void ppo_move(const ppo_params *p, uint64_t seed, uint32_t iter, uint32_t n,
 		default: break;
 		}
 		cell_out[i] = y * GX + x;
-		en_out[i] = (en & PPO_TYPE_BIT) | (e - 1);
+		en_out[i] = (en & PPO_TYPE_BIT) | e1;
 	}
 	free(rank);
 }
@@ -256,6 +266,7 @@ int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
 	uint32_t *dice = malloc(sizeof(uint32_t) * (n ? n : 1));
 	uint64_t out = 0;
 	int64_t ret;
+	const uint32_t emask = ppo_energy_mask(p);
 
 	uint32_t lo = 0;
 	while (lo < n) {
@@ -282,7 +293,7 @@ int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
 			if (type_of(en[s])) {
 				/* Wolf k eats the k-th sheep in order, if there is one
 				 * (pp_cpu.cl:721-763). */
-				if (wb < S) fin[s] += p->wolves_gain;
+				if (wb < S) fin[s] = (fin[s] + p->wolves_gain) & emask;
 				wb++;
 				acts = 1;
 				thr = p->wolves_thr; prob = p->wolves_prob;
@@ -294,7 +305,7 @@ int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
 				sb++;
 				if (acts && g == 0) {
 					g = p->grass_restart;
-					fin[s] += p->sheep_gain;
+					fin[s] = (fin[s] + p->sheep_gain) & emask;
 				}
 				thr = p->sheep_thr; prob = p->sheep_prob;
 			}

@@ -30,12 +30,19 @@
 extern "C" {
 #endif
 
-/* Same layout as PPParameters / PPStatistics of the library ABI. */
+/* The fields of PPParameters (same order), then the width of the agents'
+ * energy field: energy arithmetic is modulo 2^energy_bits, as the
+ * reference's packed agents do it (pp_gpu.cl:150-316: 16 bits in its
+ * 64-bit agents, 11 bits in its 32-bit ones); 0 means 30 bits. */
 typedef struct ppo_params {
 	uint32_t init_sheep, sheep_gain, sheep_thr, sheep_prob;
 	uint32_t init_wolves, wolves_gain, wolves_thr, wolves_prob;
 	uint32_t grass_restart, grid_x, grid_y, grid_xy, iters;
+	uint32_t energy_bits;
 } ppo_params;
+
+/* Energy field mask of p (2^energy_bits - 1). */
+uint32_t ppo_energy_mask(const ppo_params *p);
 
 typedef struct ppo_stats {
 	uint32_t sheep, wolves, grass, errors;

@@ -20,7 +20,7 @@ class OParams(C.Structure):
     _fields_ = [(f, C.c_uint32) for f in (
         "init_sheep", "sheep_gain", "sheep_thr", "sheep_prob", "init_wolves",
         "wolves_gain", "wolves_thr", "wolves_prob", "grass_restart", "grid_x",
-        "grid_y", "grid_xy", "iters")]
+        "grid_y", "grid_xy", "iters", "energy_bits")]
 
 
 class OStats(C.Structure):
@@ -74,9 +74,10 @@ def lib():
     return _lib
 
 
-def oparams(p):
+def oparams(p, energy_bits=0):
     """Convert a PPParameters (or any object/dict with the reference field
-    names) to the oracle's struct."""
+    names) to the oracle's struct; energy_bits = width of the energy field
+    (11 and 16 as the reference's 32- and 64-bit agents; 0 = 30)."""
     get = (lambda k: p[k]) if isinstance(p, dict) else (lambda k: getattr(p, k))
     o = OParams()
     o.init_sheep = get("init_sheep")
@@ -92,6 +93,7 @@ def oparams(p):
     o.grid_y = get("grid_y")
     o.grid_xy = o.grid_x * o.grid_y
     o.iters = get("iters")
+    o.energy_bits = energy_bits
     return o
 
 
@@ -114,10 +116,10 @@ def draw(w, n):
     return lib().ppo_draw(w, n)
 
 
-def run(p, seed, iters=None):
+def run(p, seed, iters=None, energy_bits=0):
     """Stats rows (iters+1) as an (iters+1, 6) uint64 array:
     sheep, wolves, grass, sheep_en, wolves_en, grass_en."""
-    o = oparams(p)
+    o = oparams(p, energy_bits)
     iters = o.iters if iters is None else iters
     rows = (OStats * (iters + 1))()
     rc = lib().ppo_run(C.byref(o), seed, iters, rows)
@@ -129,8 +131,8 @@ def run(p, seed, iters=None):
 class State:
     """Step-by-step oracle state (for state-level comparisons)."""
 
-    def __init__(self, p, seed, capacity=0):
-        self.o = oparams(p)
+    def __init__(self, p, seed, capacity=0, energy_bits=0):
+        self.o = oparams(p, energy_bits)
         self._h = lib().ppo_create(C.byref(self.o), seed, capacity)
         if not self._h:
             raise MemoryError("oracle allocation failed")
@@ -168,8 +170,8 @@ class State:
         self.close()
 
 
-def move(p, seed, it, cell, en):
-    o = oparams(p)
+def move(p, seed, it, cell, en, energy_bits=0):
+    o = oparams(p, energy_bits)
     cell = np.ascontiguousarray(cell, np.uint32)
     en = np.ascontiguousarray(en, np.uint32)
     co = np.zeros_like(cell)
@@ -180,8 +182,8 @@ def move(p, seed, it, cell, en):
     return co, eo
 
 
-def act(p, seed, it, cell, en, grass, cap):
-    o = oparams(p)
+def act(p, seed, it, cell, en, grass, cap, energy_bits=0):
+    o = oparams(p, energy_bits)
     cell = np.ascontiguousarray(cell, np.uint32)
     en = np.ascontiguousarray(en, np.uint32)
     g = np.array(grass, np.uint16)

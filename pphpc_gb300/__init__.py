@@ -75,7 +75,8 @@ class PPOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("max_agents", C.c_uint32),
                 ("tile_cells", C.c_uint32), ("sort_digit_bits", C.c_uint32),
                 ("use_graph", C.c_uint32), ("sort_pipeline", C.c_uint32),
-                ("autotune", C.c_uint32), ("ss_from", C.c_uint32)]
+                ("autotune", C.c_uint32), ("ss_from", C.c_uint32),
+                ("agent_size", C.c_uint32)]
 
 
 class PPRunDesc(C.Structure):
@@ -86,13 +87,14 @@ class PPBatchOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("pool_factor", C.c_uint32),
                 ("tile_cells", C.c_uint32), ("sort_digit_bits", C.c_uint32),
                 ("use_graph", C.c_uint32), ("stats_chunk", C.c_uint32),
-                ("autotune", C.c_uint32)]
+                ("autotune", C.c_uint32), ("agent_size", C.c_uint32)]
 
 
 class PPServeOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("mem_budget_bytes", C.c_uint64),
                 ("max_runs", C.c_uint32), ("pool_factor", C.c_uint32),
-                ("stats_chunk", C.c_uint32), ("ss_from", C.c_uint32)]
+                ("stats_chunk", C.c_uint32), ("ss_from", C.c_uint32),
+                ("agent_size", C.c_uint32)]
 
 
 class PPServeEvent(C.Structure):
@@ -239,11 +241,13 @@ def format_row(row, params):
 
 
 class Simulation:
-    """One PPHPC run on the GPU (pp_sim_* of the C ABI)."""
+    """One PPHPC run on the GPU (pp_sim_* of the C ABI). agent_size = the
+    reference's -a/--agent-size: 64 or 32 give its 16- or 11-bit energy
+    field, 0 a 30-bit one (pp_opts.agent_size)."""
 
     def __init__(self, params, seed=0, device=0, max_agents=0, tile_cells=0,
                  digit_bits=0, use_graph=True, sort_pipeline=False, autotune=False,
-                 ss_from=1000, _restore=None):
+                 ss_from=1000, agent_size=0, _restore=None):
         L = lib()
         o = PPOpts()
         L.pp_opts_default(C.byref(o))
@@ -255,6 +259,7 @@ class Simulation:
         o.sort_pipeline = 1 if sort_pipeline else 0
         o.autotune = 1 if autotune else 0
         o.ss_from = ss_from
+        o.agent_size = agent_size
         self.params = params
         self._h = C.c_void_p()
         if _restore is not None:
@@ -373,7 +378,7 @@ def run(params, seed=0, iters=None, **kw):
 
 
 def batch_run(runs, pool_factor=4, tile_cells=0, digit_bits=0, use_graph=True,
-              stats_chunk=1024, device=0, autotune=False):
+              stats_chunk=1024, device=0, autotune=False, agent_size=0):
     """Run many independent simulations in one world. `runs` is a list of
     (PPParameters, seed); returns a list of row lists."""
     L = lib()
@@ -390,6 +395,7 @@ def batch_run(runs, pool_factor=4, tile_cells=0, digit_bits=0, use_graph=True,
     o.use_graph = 1 if use_graph else 0
     o.stats_chunk = stats_chunk
     o.autotune = 1 if autotune else 0
+    o.agent_size = agent_size
     out = [None] * len(runs)
 
     def cb(r, rows, n, user):
@@ -404,7 +410,7 @@ class Server:
     """Continuous-batching server (pp_serve_* of the C ABI)."""
 
     def __init__(self, mem_budget_bytes=8 << 30, max_runs=256, pool_factor=4,
-                 stats_chunk=64, device=0, ss_from=1000):
+                 stats_chunk=64, device=0, ss_from=1000, agent_size=0):
         L = lib()
         o = PPServeOpts()
         L.pp_serve_opts_default(C.byref(o))
@@ -414,6 +420,7 @@ class Server:
         o.pool_factor = pool_factor
         o.stats_chunk = stats_chunk
         o.ss_from = ss_from
+        o.agent_size = agent_size
         self._h = C.c_void_p()
         _check(L.pp_serve_create(C.byref(o), C.byref(self._h)), "pp_serve_create")
 

@@ -39,14 +39,14 @@ __host__ __device__ __forceinline__ int32_t src_offset(uint32_t dir,
 	}
 }
 
-/* Energy loss, death and toroidal random walk of one agent of rank k in
- * its cell (pp_gpu.cl:756-819). */
+/* Energy loss (modulo the energy field), death at 0 and toroidal random
+ * walk of one agent of rank k in its cell (pp_gpu.cl:756-819). */
 __device__ __forceinline__ void move_one(const RunDev &run, uint32_t key,
 	uint32_t val, uint32_t k, uint32_t t, uint32_t dead_key,
 	uint32_t &nk, uint32_t &nv)
 {
-	uint32_t e = val & ENERGY_MASK;
-	if (e <= 1) {
+	const uint32_t e1 = ((val & ENERGY_MASK) - 1) & run.emask;
+	if (e1 == 0) {
 		nk = dead_key;
 		nv = val & TYPE_BIT;
 		return;
@@ -54,7 +54,7 @@ __device__ __forceinline__ void move_one(const RunDev &run, uint32_t key,
 	uint32_t lc = key - run.cbase;
 	u4 r = rng(run.seed_lo, run.seed_hi, lc, t, STREAM_MOVE, k);
 	nk = run.cbase + move_dir(run, lc, draw(r.x, 5));
-	nv = val - 1;
+	nv = (val & TYPE_BIT) | e1;
 }
 
 __device__ __forceinline__ bool run_live(const RunDev &run, uint32_t t)
@@ -67,6 +67,7 @@ struct ActParams {
 	uint32_t sheep_gain, sheep_thr, sheep_prob;
 	uint32_t wolves_gain, wolves_thr, wolves_prob;
 	uint32_t restart;
+	uint32_t emask;    /* energy gains are modulo the energy field */
 };
 
 /* Actions of the agents of one cell, entries [p, e) of the tile's agent
@@ -78,8 +79,8 @@ struct ActParams {
  * sheep takes live grass; every acting agent may reproduce) in closed form:
  * the k-th wolf eats the k-th sheep, and a sheep acts iff the wolves before
  * it are no more than the sheep before it.
- * On return LV[j] holds type | final energy (energy 0 = eaten) and LD[j]
- * the newborn's energy (0 = none). */
+ * On return LV[j] holds type | final energy, or type | EATEN_BIT, and
+ * LD[j] the newborn's energy (0 = none). */
 __device__ __forceinline__ void act_cell(uint32_t p, uint32_t e,
 	uint32_t *LV, const uint32_t *LP, uint32_t *LD, const ActParams &ap,
 	uint32_t &g)
@@ -95,7 +96,7 @@ __device__ __forceinline__ void act_cell(uint32_t p, uint32_t e,
 		} else {
 			if (g == 0) {
 				g = ap.restart;
-				en += ap.sheep_gain;
+				en = (en + ap.sheep_gain) & ap.emask;
 			}
 			thr = ap.sheep_thr;
 			prob = ap.sheep_prob;
@@ -136,7 +137,7 @@ __device__ __forceinline__ void act_cell(uint32_t p, uint32_t e,
 		bool acts, eaten = false;
 		uint32_t thr, prob;
 		if (tb) {
-			if (wb < S) en += ap.wolves_gain;
+			if (wb < S) en = (en + ap.wolves_gain) & ap.emask;
 			wb++;
 			acts = true;
 			thr = ap.wolves_thr;
@@ -147,7 +148,7 @@ __device__ __forceinline__ void act_cell(uint32_t p, uint32_t e,
 			sb++;
 			if (acts && g == 0) {
 				g = ap.restart;
-				en += ap.sheep_gain;
+				en = (en + ap.sheep_gain) & ap.emask;
 			}
 			thr = ap.sheep_thr;
 			prob = ap.sheep_prob;
@@ -157,7 +158,7 @@ __device__ __forceinline__ void act_cell(uint32_t p, uint32_t e,
 			kid = en >> 1;
 			en -= kid;
 		}
-		LV[best] = tb | (eaten ? 0u : en);
+		LV[best] = tb | (eaten ? EATEN_BIT : en);
 		LD[best] = kid;
 		lp = LP[best];
 		ls = best;

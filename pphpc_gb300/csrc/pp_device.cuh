@@ -14,8 +14,10 @@
  *   key[i] = global cell index (y * grid_x + x + run cell base), or the
  *            world's dead sentinel (= number of padded cells) after a move
  *            that killed the agent;
- *   val[i] = type << 31 | energy (31 bits).
- * This replaces the reference's packed 64-bit agent (pp_gpu.cl:150-234):
+ *   val[i] = type << 31 | energy (the run's energy field width: 11 or
+ *            16 bits as the reference's 32- and 64-bit agents, else 30
+ *            bits; energy arithmetic is modulo 2^width as there).
+ * This replaces the reference's packed agents (pp_gpu.cl:150-316):
  * the cell is the sort key, so the radix sort moves 8 bytes per agent and
  * sorts only ceil(log2(cells + 1)) bits.
  */
@@ -28,6 +30,15 @@ namespace pp {
 
 constexpr uint32_t TYPE_BIT = 0x80000000u;
 constexpr uint32_t ENERGY_MASK = 0x7fffffffu;
+/* Marks an agent eaten in the act phase's per-agent words (above every
+ * energy field width). */
+constexpr uint32_t EATEN_BIT = 0x40000000u;
+
+/* Energy field mask for a width of bits (11, 16 or 30). */
+__host__ __device__ __forceinline__ uint32_t energy_mask_of(uint32_t bits)
+{
+	return bits >= 30 ? 0x3fffffffu : (1u << bits) - 1;
+}
 
 enum : uint32_t {
 	STREAM_INIT_CELL = 0,
@@ -150,6 +161,7 @@ struct RunDev {
 	uint32_t active;           /* 0 = finished or empty slot               */
 	uint32_t fbase;            /* this run's regrowth histogram (restart+1 slots) */
 	uint32_t ss_from;          /* focal measures: steady state is t > ss_from */
+	uint32_t emask;            /* energy field mask (2^width - 1)          */
 	fastdiv gxdiv;
 };
 

@@ -393,6 +393,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		ap.sheep_prob = run.sheep_prob; ap.wolves_gain = run.wolves_gain;
 		ap.wolves_thr = run.wolves_thr; ap.wolves_prob = run.wolves_prob;
 		ap.restart = run.restart;
+		ap.emask = run.emask;
 		const uint16_t t16 = (uint16_t) t;
 		for (uint32_t j = tid; j < m; j += NT) {
 			const uint32_t lc = LK[j];
@@ -421,7 +422,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		for (uint32_t j = ja; j < jb; j++) {
 			const uint32_t v = LV[j], kd = LD[j];
 			const uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
-			if (en) {
+			if (!(v & EATEN_BIT)) {
 				cnt++;
 				if (tb) { wolves++; wen += en; } else { sheep++; sen += en; }
 			}
@@ -443,7 +444,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		uint32_t o = step_excl_scan<NT>(cnt, &total);
 		for (uint32_t j = ja; j < jb; j++) {
 			LP[j] = o;
-			if (LV[j] & ENERGY_MASK) {
+			if (!(LV[j] & EATEN_BIT)) {
 				if (in_smem) OUTJ16[o] = (uint16_t) j; else OUTJ32[o] = j;
 				o++;
 			}
@@ -498,7 +499,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		if (!live_move) {
 			code = DIR_PARKED;
 			cls = CLS_GRAVE;
-		} else if (en <= 1) {
+		} else if (((en - 1) & run.emask) == 0) {
 			code = DIR_DEAD;
 			cls = CLS_GRAVE;
 		} else {
@@ -565,7 +566,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 				const uint32_t code = (d >> REC_DIR_SHIFT) & 7u;
 				cls = d >> 16;
 				key = (d & 0xffffu) | (rank << REC_RANK_SHIFT);
-				val = code >= DIR_PARKED ? (tb | en) : (tb | (en - 1));
+				val = code >= DIR_PARKED ? (tb | en) : (tb | ((en - 1) & run.emask));
 				const uint32_t pos = warp_agg_add(s_cpos, cls);
 				if (cls != NCLS) {
 					kGo[pos] = key;
@@ -583,7 +584,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 				const uint32_t dt = dg >> w.log_tile;
 				cls = dt == tile ? CLS_OWN : class_find(s_tbl, dt);
 				key = (dg & lcmask) | (code << REC_DIR_SHIFT) | (rank << REC_RANK_SHIFT);
-				val = tb | (en - 1);
+				val = tb | ((en - 1) & run.emask);
 			}
 			if (cls == CLS_NONE || rank > REC_RANK_MAX) cls = NCLS;
 			const uint32_t pos = warp_agg_add(s_cpos, cls);

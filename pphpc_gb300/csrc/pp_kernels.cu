@@ -275,6 +275,7 @@ __global__ void __launch_bounds__(ACT_THREADS, 5) k_act(WorldDev w,
 	ap.sheep_prob = run.sheep_prob; ap.wolves_gain = run.wolves_gain;
 	ap.wolves_thr = run.wolves_thr; ap.wolves_prob = run.wolves_prob;
 	ap.restart = run.restart;
+	ap.emask = run.emask;
 	const uint32_t c0 = tile << w.log_tile;
 	const uint32_t lt0 = c0 - cbase;          /* run-local index of the tile start */
 	const uint32_t a0 = w.tile_off[tile], a1 = w.tile_off[tile + 1];
@@ -391,7 +392,7 @@ __global__ void __launch_bounds__(ACT_THREADS, 5) k_act(WorldDev w,
 	const uint32_t ja = min(tid * ch, m), jb = min(ja + ch, m);
 	uint32_t cnt = 0;
 	for (uint32_t j = ja; j < jb; j++)
-		cnt += ((LV[j] & ENERGY_MASK) != 0) + (LD[j] != 0);
+		cnt += ((LV[j] & EATEN_BIT) == 0) + (LD[j] != 0);
 	uint32_t total;
 	const uint32_t excl = block_excl_scan(cnt, &total);
 	const uint32_t rs = 2 * a0;
@@ -405,7 +406,7 @@ __global__ void __launch_bounds__(ACT_THREADS, 5) k_act(WorldDev w,
 	for (uint32_t j = ja; j < jb; j++) {
 		const uint32_t v = LV[j], k = LK[j] + c0, kd = LD[j];
 		const uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
-		if (en) {
+		if (!(v & EATEN_BIT)) {
 			w.kR[o] = k;
 			w.vR[o] = v;
 			o++;
@@ -720,7 +721,7 @@ __global__ void k_init_agents(RunDev run, uint32_t *k, uint32_t *v,
 		uint32_t x = draw(r.x, run.gx), y = draw(r.y, run.gy);
 		bool wolf = a >= n_sheep;
 		uint32_t gain = wolf ? run.wolves_gain : run.sheep_gain;
-		uint32_t e = 1 + draw(r.z, 2 * gain);
+		uint32_t e = (1 + draw(r.z, 2 * gain)) & run.emask;
 		k[base + a] = run.cbase + y * run.gx + x;
 		v[base + a] = (wolf ? TYPE_BIT : 0u) | e;
 	}

@@ -3,11 +3,13 @@
  * (opencl/pp/pp_gpu.c:1700-1946, options pp_gpu.c:310-410).
  *
  *   pp_gb300 [-p PARAMS] [-s STATS] [-r SEED] [-d DEVICE] [-m MAX_AGENTS]
- *            [--iters N] [-i PROF_FILE] [-t TILE] [--digit-bits B]
- *            [--no-graph] [--dump TYPE]
+ *            [-a AGENT_SIZE] [--iters N] [-i PROF_FILE] [-t TILE]
+ *            [--digit-bits B] [--no-graph] [--dump TYPE]
  *
- * -p/-s/-r/-d/-m keep the reference's meaning and defaults (config.txt,
- * stats.txt, seed 0, device 0, agent pool); --iters overrides ITERS from
+ * -p/-s/-r/-d/-m/-a keep the reference's meaning and defaults (config.txt,
+ * stats.txt, seed 0, device 0, agent pool, 64-bit agents: -a sets the
+ * width of the energy field, 16 bits for 64 and 11 bits for 32, with the
+ * reference's modular energy arithmetic); --iters overrides ITERS from
  * the parameters file (the reference has no such knob: -i there is the
  * profiling export, kept here as a two-column kernel-time file). --dump
  * writes dump_agents.txt and dump_cells.txt after every iteration in the
@@ -34,8 +36,8 @@ static void usage(const char *argv0)
 {
 	fprintf(stderr,
 		"Usage: %s [-p FILE] [-s FILE] [-r SEED] [-d INDEX] [-m MAX]\n"
-		"          [--iters N] [-i FILE] [-t TILE] [--digit-bits B] [--no-graph]\n"
-		"          [--dump TYPE]\n",
+		"          [-a 32|64] [--iters N] [-i FILE] [-t TILE] [--digit-bits B]\n"
+		"          [--no-graph] [--dump TYPE]\n",
 		argv0);
 }
 
@@ -47,12 +49,14 @@ int main(int argc, char **argv)
 	int dump_type = -1;
 	pp_opts opts;
 	pp_opts_default(&opts);
+	long agent_size = 64;
 	static struct option longopts[] = {
 		{"params", required_argument, 0, 'p'},
 		{"stats", required_argument, 0, 's'},
 		{"rng-seed", required_argument, 0, 'r'},
 		{"device", required_argument, 0, 'd'},
 		{"max-agents", required_argument, 0, 'm'},
+		{"agent-size", required_argument, 0, 'a'},
 		{"prof-agg", required_argument, 0, 'i'},
 		{"iters", required_argument, 0, 'I'},
 		{"tile", required_argument, 0, 't'},
@@ -63,13 +67,14 @@ int main(int argc, char **argv)
 		{0, 0, 0, 0}
 	};
 	int c;
-	while ((c = getopt_long(argc, argv, "p:s:r:d:m:i:t:h", longopts, NULL)) != -1) {
+	while ((c = getopt_long(argc, argv, "p:s:r:d:m:a:i:t:h", longopts, NULL)) != -1) {
 		switch (c) {
 		case 'p': params_file = optarg; break;
 		case 's': stats_file = optarg; break;
 		case 'r': seed = strtoll(optarg, NULL, 0); break;
 		case 'd': opts.device = atoi(optarg); break;
 		case 'm': opts.max_agents = (uint32_t) strtoul(optarg, NULL, 0); break;
+		case 'a': agent_size = strtol(optarg, NULL, 0); break;
 		case 'i': prof_file = optarg; break;
 		case 'I': iters_override = strtoll(optarg, NULL, 0); break;
 		case 't': opts.tile_cells = (uint32_t) strtoul(optarg, NULL, 0); break;
@@ -84,6 +89,12 @@ int main(int argc, char **argv)
 		fprintf(stderr, "Error: This program does not accept non-option arguments.\n");
 		return PP_UNKNOWN_ARGS;
 	}
+	if (agent_size != 32 && agent_size != 64) {
+		fprintf(stderr, "Error: The -a (--agent-size) parameter must be "
+			"either 32 or 64.\n");
+		return PP_INVALID_ARGS;
+	}
+	opts.agent_size = (uint32_t) agent_size;
 	char msg[256] = "";
 	PPParameters params;
 	int rc = pp_load_params(&params, params_file, msg, sizeof(msg));
@@ -102,6 +113,12 @@ int main(int argc, char **argv)
 	if (!rows) return PP_OUT_OF_RESOURCES;
 	double t0 = now_s();
 	pp_sim *sim = NULL;
+	if (agent_size == 32 && (params.grid_x > 1024 || params.grid_y > 1024)) {
+		fprintf(stderr, "Error: 32-bit agents hold grid coordinates up to "
+			"1023; use -a 64 for this grid.\n");
+		free(rows);
+		return PP_INVALID_ARGS;
+	}
 	rc = pp_sim_create(&params, (uint64_t) seed, &opts, &sim);
 	if (rc) {
 		fprintf(stderr, "Error: unable to create simulation (%d)\n", rc);

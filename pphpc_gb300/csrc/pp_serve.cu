@@ -80,6 +80,8 @@ extern "C" int pp_serve_create(const pp_serve_opts *opts, pp_server **out)
 	if (opts) o = *opts;
 	else pp_serve_opts_default(&o);
 	if (o.max_runs == 0 || o.max_runs > 60000) return PP_INVALID_ARGS;
+	if (o.agent_size != 0 && o.agent_size != 32 && o.agent_size != 64)
+		return PP_INVALID_ARGS;
 	pp_server *srv = new (std::nothrow) pp_server();
 	if (!srv) return PP_OUT_OF_RESOURCES;
 	srv->opts = o;
@@ -138,6 +140,8 @@ extern "C" int pp_serve_submit(pp_server *srv, const pp_run_desc *run,
 	rq.spec.seed = run->seed;
 	rq.spec.iters = p.iters;
 	rq.spec.ss_from = srv->opts.ss_from;
+	rc = agent_energy_bits(srv->opts.agent_size, p, &rq.spec.energy_bits);
+	if (rc) return rc;
 	rq.reserve = reservation(rq.spec, srv->opts.pool_factor ? srv->opts.pool_factor : 4);
 	uint64_t tiles_needed = ((uint64_t) p.grid_xy + 1023) / 1024;
 	if (rq.reserve > srv->cap || tiles_needed > srv->max_tiles)

@@ -109,8 +109,22 @@ static RunDev make_run(const RunSpec &s, uint32_t first_tile,
 	r.active = 1;
 	r.fbase = fbase;
 	r.ss_from = s.ss_from;
+	r.emask = energy_mask_of(s.energy_bits);
 	r.gxdiv = fastdiv_make(s.p.grid_x);
 	return r;
+}
+
+int agent_energy_bits(uint32_t agent_size, const PPParameters &p, uint32_t *bits)
+{
+	switch (agent_size) {
+	case 0: *bits = 30; return PP_SUCCESS;
+	case 64: *bits = 16; return PP_SUCCESS;
+	case 32:
+		if (p.grid_x > 1024 || p.grid_y > 1024) return PP_INVALID_ARGS;
+		*bits = 11;
+		return PP_SUCCESS;
+	default: return PP_INVALID_ARGS;
+	}
 }
 
 int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
@@ -356,7 +370,7 @@ int World::load_run_state(const RunSpec &spec, const RunDev &run, uint32_t base,
 		if (spec.init_cell[i] >= cells) return PP_INVALID_ARGS;
 		if (i && spec.init_cell[i] < spec.init_cell[i - 1]) return PP_INVALID_ARGS;
 		const uint32_t v = spec.init_val[i], e = v & ENERGY_MASK;
-		if (e == 0) return PP_INVALID_ARGS;
+		if (e > run.emask) return PP_INVALID_ARGS;
 		kc[i] = run.cbase + spec.init_cell[i];
 		if (v & TYPE_BIT) { st.wolves++; st.wolves_en += e; }
 		else { st.sheep++; st.sheep_en += e; }
@@ -889,6 +903,7 @@ struct pp_sim {
 	uint64_t seed;
 	PPStatistics stats0;
 	uint32_t iter0 = 0;     /* iteration the simulation was restored at */
+	uint32_t agent_size = 0; /* pp_opts.agent_size it was created with */
 };
 
 extern "C" void pp_opts_default(pp_opts *o)
@@ -917,10 +932,14 @@ static int sim_create(const PPParameters *params, uint64_t seed,
 	pp_opts o;
 	if (opts) o = *opts;
 	else pp_opts_default(&o);
+	uint32_t ebits = 30;
+	rc = agent_energy_bits(o.agent_size, p, &ebits);
+	if (rc) return rc;
 	pp_sim *sim = new (std::nothrow) pp_sim();
 	if (!sim) return PP_OUT_OF_RESOURCES;
 	sim->params = p;
 	sim->seed = seed;
+	sim->agent_size = o.agent_size;
 	WorldConfig cfg;
 	cfg.device = o.device;
 	uint64_t n0 = (uint64_t) p.init_sheep + p.init_wolves;
@@ -949,6 +968,7 @@ static int sim_create(const PPParameters *params, uint64_t seed,
 	runs[0].seed = seed;
 	runs[0].iters = 0xffffffffu;
 	runs[0].ss_from = o.ss_from;
+	runs[0].energy_bits = ebits;
 	sim->iter0 = spec0 ? spec0->start_iter : 0;
 	rc = sim->world.create(runs, cfg);
 	if (rc == PP_SUCCESS) rc = sim->world.read_rows(0, 0, 0, &sim->stats0);
@@ -967,10 +987,13 @@ extern "C" int pp_sim_create(const PPParameters *params, uint64_t seed,
 	return sim_create(params, seed, opts, nullptr, out);
 }
 
-/* Snapshot file: magic, parameters, seed, iteration, agent count, then the
- * agents' run-local cells and type | energy words in canonical order and
- * the grid's grass countdowns (native byte order). */
-static const char SNAP_MAGIC[8] = {'P', 'P', 'S', 'N', 'A', 'P', '0', '1'};
+/* Snapshot file: magic, parameters, seed, iteration, agent count, agent
+ * size (pp_opts.agent_size), then the agents' run-local cells and type |
+ * energy words in canonical order and the grid's grass countdowns (native
+ * byte order). Files of the first version (magic ...01) have no agent size
+ * field; they restore with the caller's. */
+static const char SNAP_MAGIC[8] = {'P', 'P', 'S', 'N', 'A', 'P', '0', '2'};
+static const char SNAP_MAGIC_V1[8] = {'P', 'P', 'S', 'N', 'A', 'P', '0', '1'};
 
 extern "C" int pp_sim_snapshot_save(pp_sim *sim, const char *path)
 {
@@ -994,6 +1017,7 @@ extern "C" int pp_sim_snapshot_save(pp_sim *sim, const char *path)
 		&& fwrite(&sim->seed, 8, 1, f) == 1
 		&& fwrite(&iter, 4, 1, f) == 1
 		&& fwrite(&n, 4, 1, f) == 1
+		&& fwrite(&sim->agent_size, 4, 1, f) == 1
 		&& (n == 0 || fwrite(cell.data(), 4, n, f) == n)
 		&& (n == 0 || fwrite(en.data(), 4, n, f) == n)
 		&& fwrite(grass.data(), 2, grass.size(), f) == grass.size();
@@ -1011,9 +1035,15 @@ extern "C" int pp_sim_restore(const char *path, const pp_opts *opts, pp_sim **ou
 	PPParameters p;
 	uint64_t seed = 0;
 	uint32_t iter = 0, n = 0;
-	bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, SNAP_MAGIC, 8) == 0
+	pp_opts o;
+	if (opts) o = *opts;
+	else pp_opts_default(&o);
+	bool ok = fread(magic, 1, 8, f) == 8;
+	const bool v1 = ok && memcmp(magic, SNAP_MAGIC_V1, 8) == 0;
+	ok = ok && (v1 || memcmp(magic, SNAP_MAGIC, 8) == 0)
 		&& fread(&p, sizeof(p), 1, f) == 1 && fread(&seed, 8, 1, f) == 1
 		&& fread(&iter, 4, 1, f) == 1 && fread(&n, 4, 1, f) == 1
+		&& (v1 || fread(&o.agent_size, 4, 1, f) == 1)
 		&& p.grid_x > 0 && p.grid_y > 0 && p.grid_x <= 65535 && p.grid_y <= 65535
 		&& n < 0x80000000u;
 	std::vector<uint32_t> cell, en;
@@ -1034,7 +1064,7 @@ extern "C" int pp_sim_restore(const char *path, const pp_opts *opts, pp_sim **ou
 	spec.init_grass = grass.data();
 	spec.init_n = n;
 	spec.start_iter = iter;
-	return sim_create(&p, seed, opts, &spec, out);
+	return sim_create(&p, seed, &o, &spec, out);
 }
 
 void pp::focal_export(const FocalDev &f, pp_focal *out)
@@ -1378,6 +1408,8 @@ extern "C" int pp_batch_run(const pp_run_desc *runs, int n_runs,
 		specs[r].p = p;
 		specs[r].seed = runs[r].seed;
 		specs[r].iters = p.iters;
+		rc = agent_energy_bits(o.agent_size, p, &specs[r].energy_bits);
+		if (rc) return rc;
 		n0 += (uint64_t) p.init_sheep + p.init_wolves;
 		cells += p.grid_xy;
 		max_iters = std::max(max_iters, p.iters);

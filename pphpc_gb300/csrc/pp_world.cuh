@@ -25,11 +25,16 @@ struct RunSpec {
 	uint32_t init_n = 0;
 	uint32_t start_iter = 0;
 	uint32_t ss_from = 1000;  /* focal measures: steady state is t > ss_from */
+	uint32_t energy_bits = 30; /* energy field width (11, 16 or 30)        */
 	uint64_t agents() const
 	{
 		return init_val ? (uint64_t) init_n : (uint64_t) p.init_sheep + p.init_wolves;
 	}
 };
+
+/* Energy field width for the reference's agent size (0, 32 or 64) on a
+ * grid of p (32-bit agents hold 10-bit coordinates, pp_gpu.cl:236-316). */
+int agent_energy_bits(uint32_t agent_size, const PPParameters &p, uint32_t *bits);
 
 struct WorldConfig {
 	int device = 0;

@@ -55,14 +55,20 @@ def test_move_matches_oracle(gx, gy):
 
 
 def test_move_energy_death():
+    """Energy 1 dies in the move; energy 0 (only reachable by a gain that
+    wraps the energy field) wraps to the field maximum and lives, as the
+    reference's modular decrement does (pp_gpu.cl:805-810)."""
     p = params(20)
     cell = np.arange(6, dtype=np.uint32)
     en = np.array([0, 1, 2, 0x80000000, 0x80000001, 0x80000002], np.uint32)
     gc, ge = pp.move(p, 1, 1, cell, en)
     dead = p.grid_x * p.grid_y
-    assert list(gc[[0, 1, 3, 4]]) == [dead] * 4
+    assert list(gc[[1, 4]]) == [dead] * 2
     assert ge[2] == 1 and ge[5] == 0x80000001
-    assert gc[2] < dead and gc[5] < dead
+    assert ge[0] == 0x3fffffff and ge[3] == 0x80000000 | 0x3fffffff
+    assert all(gc[[0, 2, 3, 5]] < dead)
+    oc, oe = orc.move(p, 1, 1, cell, en)
+    assert np.array_equal(gc, oc) and np.array_equal(ge, oe)
 
 
 def _stable(keys, vals):
