@@ -70,99 +70,70 @@ struct ActParams {
 	uint32_t emask;    /* energy gains are modulo the energy field */
 };
 
-/* Actions of the agents of one cell, entries [p, e) of the tile's agent
- * list in cell-list order, in increasing (priority, rank) order; on entry
- * LP[j] / LD[j] hold the priority and the dice of the agent of rank j - p,
- * drawn from Philox({cell, t, ACT, rank}). This is the sequential semantics
- * of pp_cpu.cl:640-848 (wolves eat the first not-yet-eaten sheep of the
- * cell; a sheep acts only if not eaten before its turn; the first acting
- * sheep takes live grass; every acting agent may reproduce) in closed form:
- * the k-th wolf eats the k-th sheep, and a sheep acts iff the wolves before
- * it are no more than the sheep before it.
- * On return LV[j] holds type | final energy, or type | EATEN_BIT, and
- * LD[j] the newborn's energy (0 = none). */
-__device__ __forceinline__ void act_cell(uint32_t p, uint32_t e,
-	uint32_t *LV, const uint32_t *LP, uint32_t *LD, const ActParams &ap,
-	uint32_t &g)
+/* Actions of agent j of one cell, whose list is entries [p, e) of the
+ * tile's agent list; LP[i] holds the priority of the agent of rank i - p,
+ * drawn from Philox({cell, t, ACT, rank}), and dice that agent's draw of
+ * U[0, 100) from the same counter. This is the sequential semantics of
+ * pp_cpu.cl:640-848 (agents act in increasing (priority, rank) order;
+ * wolves eat the first not-yet-eaten sheep of the cell; a sheep acts only if
+ * not eaten before its turn; the first acting sheep takes live grass; every
+ * acting agent may reproduce) in closed form, evaluated by the agent's own
+ * thread: with sb and wb the sheep and wolves before it, the k-th wolf eats
+ * the k-th sheep (a wolf gains iff wb < sheep in the cell), a sheep acts
+ * iff wb <= sb and is eaten iff sb < wolves in the cell, and it takes the
+ * cell's live grass (g0 == 0) iff it acts and no sheep before it acts.
+ * LV[i] keeps its type bit throughout, so the agents of a cell read each
+ * other's types while they write their results. On return LV[j] holds type
+ * | final energy, or type | EATEN_BIT, and *kid the newborn's energy (0 =
+ * none); the result is true iff agent j eats the grass. */
+__device__ __forceinline__ bool act_agent(uint32_t j, uint32_t p, uint32_t e,
+	uint32_t *LV, const uint32_t *LP, const ActParams &ap, uint32_t g0,
+	uint32_t dice, uint32_t *kid)
 {
+	const uint32_t v = LV[j], tb = v & TYPE_BIT;
+	uint32_t en = v & ENERGY_MASK;
+	bool acts = true, eaten = false, grass = false;
 	if (e - p == 1) {
-		/* alone in its cell: a sheep acts and is not eaten, a wolf finds
-		 * no sheep */
-		const uint32_t v = LV[p], tb = v & TYPE_BIT;
-		uint32_t en = v & ENERGY_MASK, thr, prob;
-		if (tb) {
-			thr = ap.wolves_thr;
-			prob = ap.wolves_prob;
-		} else {
-			if (g == 0) {
-				g = ap.restart;
-				en = (en + ap.sheep_gain) & ap.emask;
-			}
-			thr = ap.sheep_thr;
-			prob = ap.sheep_prob;
+		grass = !tb && g0 == 0;
+	} else {
+		const uint32_t pj = LP[j];
+		uint32_t S = 0, W = 0, sb = 0, wb = 0;
+		for (uint32_t i = p; i < e; i++) {
+			const uint32_t pi = LP[i];
+			const uint32_t before = pi < pj || (pi == pj && i < j);
+			if (LV[i] & TYPE_BIT) { W++; wb += before; }
+			else { S++; sb += before; }
 		}
-		const uint32_t kid = (en > thr && LD[p] < prob) ? en >> 1 : 0;
-		LV[p] = tb | (en - kid);
-		LD[p] = kid;
-		return;
-	}
-	uint32_t S = 0, W = 0;
-	for (uint32_t j = p; j < e; j++) {
-		if (LV[j] & TYPE_BIT) W++;
-		else S++;
-	}
-	uint32_t sb = 0, wb = 0;
-	uint32_t lp = 0;
-	uint32_t ls = 0xffffffffu; /* none selected yet */
-	const uint32_t m = e - p;
-	for (uint32_t step = 0; step < m; step++) {
-		uint32_t best = p;
-		if (m > 1) {
-			uint32_t bp = 0xffffffffu;
-			bool found = false;
-			for (uint32_t j = p; j < e; j++) {
-				uint32_t pj = LP[j];
-				bool after = (ls == 0xffffffffu) || pj > lp
-					|| (pj == lp && j > ls);
-				if (after && (!found || pj < bp)) {
-					best = j;
-					bp = pj;
-					found = true;
-				}
-			}
-		}
-		uint32_t v = LV[best];
-		uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
-		uint32_t dice = LD[best];
-		bool acts, eaten = false;
-		uint32_t thr, prob;
 		if (tb) {
 			if (wb < S) en = (en + ap.wolves_gain) & ap.emask;
-			wb++;
-			acts = true;
-			thr = ap.wolves_thr;
-			prob = ap.wolves_prob;
 		} else {
 			acts = wb <= sb;
 			eaten = sb < W;
-			sb++;
-			if (acts && g == 0) {
-				g = ap.restart;
-				en = (en + ap.sheep_gain) & ap.emask;
+			grass = acts && g0 == 0;
+			/* an earlier sheep i acts iff the wolves before it are no
+			 * more than the sheep before it */
+			for (uint32_t i = p; i < e && grass; i++) {
+				const uint32_t pi = LP[i];
+				if ((LV[i] & TYPE_BIT) || !(pi < pj || (pi == pj && i < j))) continue;
+				uint32_t s2 = 0, w2 = 0;
+				for (uint32_t q = p; q < e; q++) {
+					const uint32_t pq = LP[q];
+					if (pq < pi || (pq == pi && q < i)) {
+						if (LV[q] & TYPE_BIT) w2++;
+						else s2++;
+					}
+				}
+				if (w2 <= s2) grass = false;
 			}
-			thr = ap.sheep_thr;
-			prob = ap.sheep_prob;
 		}
-		uint32_t kid = 0;
-		if (acts && en > thr && dice < prob) {
-			kid = en >> 1;
-			en -= kid;
-		}
-		LV[best] = tb | (eaten ? EATEN_BIT : en);
-		LD[best] = kid;
-		lp = LP[best];
-		ls = best;
 	}
+	if (grass) en = (en + ap.sheep_gain) & ap.emask;
+	const uint32_t thr = tb ? ap.wolves_thr : ap.sheep_thr;
+	const uint32_t prob = tb ? ap.wolves_prob : ap.sheep_prob;
+	const uint32_t k = (acts && en > thr && dice < prob) ? en >> 1 : 0;
+	LV[j] = tb | (eaten ? EATEN_BIT : en - k);
+	*kid = k;
+	return grass;
 }
 
 struct StatAcc {

@@ -139,4 +139,20 @@ __device__ __forceinline__ T warp_sum(T v)
 	return v;
 }
 
+/* Full-warp sums with the warp reduction instruction (redux.sync). */
+__device__ __forceinline__ uint32_t warp_sum(uint32_t v)
+{
+	return __reduce_add_sync(0xffffffffu, v);
+}
+
+/* 64-bit: three 22-bit chunks, whose 32-lane sums cannot overflow 32 bits;
+ * the result is the sum modulo 2^64. */
+__device__ __forceinline__ uint64_t warp_sum(uint64_t v)
+{
+	const uint32_t s0 = __reduce_add_sync(0xffffffffu, (uint32_t) v & 0x3fffffu);
+	const uint32_t s1 = __reduce_add_sync(0xffffffffu, (uint32_t) (v >> 22) & 0x3fffffu);
+	const uint32_t s2 = __reduce_add_sync(0xffffffffu, (uint32_t) (v >> 44));
+	return (uint64_t) s0 + ((uint64_t) s1 << 22) + ((uint64_t) s2 << 44);
+}
+
 } /* namespace pp */

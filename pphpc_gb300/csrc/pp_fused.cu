@@ -273,7 +273,6 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 	}
 	uint32_t *LP = UK, *LD = UV;      /* priorities / dice, then offsets / kids */
 
-	const uint32_t cell0 = tid * CPT;
 	uint32_t eats = 0;
 	if (!ACT) {
 		for (uint32_t j = tid; j < m; j += NT) {
@@ -324,16 +323,13 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 				}
 			}
 		}
-		uint64_t multi = 0;   /* this thread's cells holding two or more agents */
 		__syncthreads();
 		if (tid == 0) w.inbox_n[(size_t) pin * w.n_tiles + tile] = 0;
 		{
 			uint32_t loc = 0;
 #pragma unroll
 			for (int q = 0; q < CPT; q++) {
-				const uint32_t c = scnt[q * NT + tid];
-				loc += c;
-				if (c > 1) multi |= 1ull << q;
+				loc += scnt[q * NT + tid];
 			}
 			uint32_t tot;
 			uint32_t run_start = step_excl_scan<NT>(loc, &tot);
@@ -348,33 +344,27 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		for (uint32_t j = tid; j < m; j += NT)
 			PERM[atomicAdd(&scnt[SLOT(UK[j] & lcmask)], 1u)] = j;
 		__syncthreads();
-		/* scnt[SLOT(c)] is now the end of cell c; put each multi-agent
-		 * cell's list in canonical order */
-		while (multi) {
-			const int q = __ffsll((long long) multi) - 1;
-			multi &= multi - 1;
-			const uint32_t c = cell0 + q;
-			const uint32_t b = c ? scnt[SLOT(c - 1)] : 0, e = scnt[SLOT(c)];
-			const uint32_t lr = lt0 + c;
-			const uint32_t y = fastdiv_div(lr, run.gxdiv), x = lr - y * run.gx;
-			for (uint32_t i = b + 1; i < e; i++) {
-				const uint32_t xj = PERM[i];
-				const int64_t kx = order_key(UK[xj], x, y, run.gx, run.gy);
-				uint32_t h = i;
-				while (h > b && order_key(UK[PERM[h - 1]], x, y, run.gx, run.gy) > kx) {
-					PERM[h] = PERM[h - 1];
-					h--;
-				}
-				PERM[h] = xj;
-			}
-		}
-#undef SLOT
-		__syncthreads();
+		/* scnt[SLOT(c)] is now the end of cell c, and cell c's agents
+		 * occupy [end of c - 1, end of c) in arrival order; each goes to
+		 * the cell's start plus its rank in canonical order, which only
+		 * an agent sharing its cell has to count */
 		for (uint32_t i = tid; i < m; i += NT) {
 			const uint32_t j = PERM[i];
-			LK[i] = UK[j] & lcmask;
-			LV[i] = UV[j];
+			const uint32_t rk = UK[j], c = rk & lcmask;
+			const uint32_t e = scnt[SLOT(c)], b = c ? scnt[SLOT(c - 1)] : 0;
+			uint32_t d = i;
+			if (e - b > 1) {
+				const uint32_t lr = lt0 + c;
+				const uint32_t y = fastdiv_div(lr, run.gxdiv), x = lr - y * run.gx;
+				const int64_t kx = order_key(rk, x, y, run.gx, run.gy);
+				d = b;
+				for (uint32_t q = b; q < e; q++)
+					d += order_key(UK[PERM[q]], x, y, run.gx, run.gy) < kx;
+			}
+			LK[d] = c;
+			LV[d] = UV[j];
 		}
+#undef SLOT
 		__syncthreads();
 		/* B: draws of every agent */
 		for (uint32_t j = tid; j < m; j += NT) {
@@ -387,7 +377,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		}
 		cp_async_wait_all();
 		__syncthreads();
-		/* C: actions, one thread per occupied cell (its first agent's) */
+		/* C: actions, one thread per agent */
 		ActParams ap;
 		ap.sheep_gain = run.sheep_gain; ap.sheep_thr = run.sheep_thr;
 		ap.sheep_prob = run.sheep_prob; ap.wolves_gain = run.wolves_gain;
@@ -397,17 +387,16 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		const uint16_t t16 = (uint16_t) t;
 		for (uint32_t j = tid; j < m; j += NT) {
 			const uint32_t lc = LK[j];
-			if (j > 0 && LK[j - 1] == lc) continue;
-			uint32_t e = j + 1;
+			uint32_t p = j, e = j + 1;
+			while (p > 0 && LK[p - 1] == lc) p--;
 			while (e < m && LK[e] == lc) e++;
 			const int32_t dd = (int16_t) (uint16_t) (sgrass[lc] - t16);
-			uint32_t gq = dd > 0 ? (uint32_t) dd : 0u;
-			const uint32_t g0 = gq;
-			act_cell(j, e, LV, LP, LD, ap, gq);
-			if (gq != g0) {
+			uint32_t kid;
+			if (act_agent(j, p, e, LV, LP, ap, dd > 0 ? (uint32_t) dd : 0u, LD[j], &kid)) {
 				w.grass[c0 + lc] = (uint16_t) (t16 + (uint16_t) ap.restart);
 				eats++;
 			}
+			LD[j] = kid;
 		}
 		__syncthreads();
 	}

@@ -356,35 +356,34 @@ __global__ void __launch_bounds__(ACT_THREADS, 5) k_act(WorldDev w,
 		LV[i] = UV[j];
 	}
 	__syncthreads();
-	/* B: draws of every agent */
+	/* B: draws of every agent, and its cell's countdown max(0, regrowth -
+	 * t) read before any sheep eats (LD = dice | countdown << 7) */
+	const uint16_t t16 = (uint16_t) t;
 	for (uint32_t j = tid; j < m; j += ACT_THREADS) {
 		const uint32_t lc = LK[j];
 		uint32_t k = 0;
 		while (k < j && LK[j - k - 1] == lc) k++;
 		u4 r = rng(seed_lo, seed_hi, lt0 + lc, t, STREAM_ACT, k);
+		const int32_t dd = (int16_t) (uint16_t) (w.grass[c0 + lc] - t16);
 		LP[j] = r.x;
-		LD[j] = draw(r.y, 100);
+		LD[j] = draw(r.y, 100) | (dd > 0 ? (uint32_t) dd << 7 : 0u);
 	}
 	__syncthreads();
-	/* C: actions, one thread per occupied cell (its first agent's). The
-	 * cell's countdown is max(0, regrowth - t); a sheep that eats sets the
-	 * regrowth to t + restart, counted for the run's regrowth histogram. */
+	/* C: actions, one thread per agent; a sheep that eats sets its cell's
+	 * regrowth to t + restart, counted for the run's regrowth histogram */
 	uint32_t eats = 0;
-	const uint16_t t16 = (uint16_t) t;
 	for (uint32_t j = tid; j < m; j += ACT_THREADS) {
 		const uint32_t lc = LK[j];
-		if (j > 0 && LK[j - 1] == lc) continue;
-		uint32_t e = j + 1;
+		uint32_t p = j, e = j + 1;
+		while (p > 0 && LK[p - 1] == lc) p--;
 		while (e < m && LK[e] == lc) e++;
-		uint16_t *gptr = w.grass + c0 + lc;
-		const int32_t dd = (int16_t) (uint16_t) (*gptr - t16);
-		uint32_t gq = dd > 0 ? (uint32_t) dd : 0u;
-		const uint32_t g0 = gq;
-		act_cell(j, e, LV, LP, LD, ap, gq);
-		if (gq != g0) {
-			*gptr = (uint16_t) (t16 + (uint16_t) ap.restart);
+		const uint32_t dg = LD[j];
+		uint32_t kid;
+		if (act_agent(j, p, e, LV, LP, ap, dg >> 7, dg & 127u, &kid)) {
+			w.grass[c0 + lc] = (uint16_t) (t16 + (uint16_t) ap.restart);
 			eats++;
 		}
+		LD[j] = kid;
 	}
 	__syncthreads();
 	/* E: outputs in list order, contiguous agent chunks per thread */
