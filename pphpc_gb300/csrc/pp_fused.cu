@@ -347,7 +347,8 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		/* scnt[SLOT(c)] is now the end of cell c, and cell c's agents
 		 * occupy [end of c - 1, end of c) in arrival order; each goes to
 		 * the cell's start plus its rank in canonical order, which only
-		 * an agent sharing its cell has to count */
+		 * an agent sharing its cell has to count. LK holds the cell in
+		 * bits 0-15 and the rank in the cell's list in bits 16-31. */
 		for (uint32_t i = tid; i < m; i += NT) {
 			const uint32_t j = PERM[i];
 			const uint32_t rk = UK[j], c = rk & lcmask;
@@ -361,17 +362,16 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 				for (uint32_t q = b; q < e; q++)
 					d += order_key(UK[PERM[q]], x, y, run.gx, run.gy) < kx;
 			}
-			LK[d] = c;
+			if (d - b > 0xffffu) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
+			LK[d] = c | (d - b) << 16;
 			LV[d] = UV[j];
 		}
 #undef SLOT
 		__syncthreads();
 		/* B: draws of every agent */
 		for (uint32_t j = tid; j < m; j += NT) {
-			const uint32_t lc = LK[j];
-			uint32_t k = 0;
-			while (k < j && LK[j - k - 1] == lc) k++;
-			u4 r = rng(seed_lo, seed_hi, lt0 + lc, t, STREAM_ACT, k);
+			const uint32_t lk = LK[j], lc = lk & 0xffffu;
+			u4 r = rng(seed_lo, seed_hi, lt0 + lc, t, STREAM_ACT, lk >> 16);
 			LP[j] = r.x;
 			LD[j] = draw(r.y, 100);
 		}
@@ -386,10 +386,10 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		ap.emask = run.emask;
 		const uint16_t t16 = (uint16_t) t;
 		for (uint32_t j = tid; j < m; j += NT) {
-			const uint32_t lc = LK[j];
-			uint32_t p = j, e = j + 1;
-			while (p > 0 && LK[p - 1] == lc) p--;
-			while (e < m && LK[e] == lc) e++;
+			const uint32_t lk = LK[j], lc = lk & 0xffffu;
+			const uint32_t p = j - (lk >> 16);
+			uint32_t e = j + 1;
+			while (e < m && (LK[e] >> 16) != 0) e++;
 			const int32_t dd = (int16_t) (uint16_t) (sgrass[lc] - t16);
 			uint32_t kid;
 			if (act_agent(j, p, e, LV, LP, ap, dd > 0 ? (uint32_t) dd : 0u, LD[j], &kid)) {
@@ -467,9 +467,10 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 			j = o;
 			nb = 0;
 		}
-		const uint32_t lc = LK[j];
-		uint32_t f = j;
-		while (f > 0 && LK[f - 1] == lc) f--;
+		const uint32_t lk = LK[j];
+		uint32_t f = j - (lk >> 16);
+		if (!ACT)
+			while (f > 0 && LK[f - 1] == lk) f--;
 		rank = o - (ACT ? LP[f] : f);
 		en = nb ? LD[j] : (LV[j] & ENERGY_MASK);
 	};
@@ -483,7 +484,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 	for (uint32_t o = tid; o < total; o += NT) {
 		uint32_t j, nb, en, rank;
 		output(o, j, nb, en, rank);
-		const uint32_t lc = LK[j];
+		const uint32_t lc = LK[j] & 0xffffu;
 		uint32_t code, cls, klo = lc;
 		if (!live_move) {
 			code = DIR_PARKED;
@@ -547,7 +548,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		for (uint32_t o = tid; o < total; o += NT) {
 			uint32_t j, nb, en, rank;
 			output(o, j, nb, en, rank);
-			const uint32_t lc = LK[j];
+			const uint32_t lc = LK[j] & 0xffffu;
 			const uint32_t tb = LV[j] & TYPE_BIT;
 			uint32_t key, val, cls;
 			if (cache) {
