@@ -35,10 +35,14 @@ namespace {
 
 static_assert(IBX == 32, "the inbox is read by one warp");
 
-/* Threads per tile CTA: 128 for sparse tiles (eight CTAs per SM), 256 when
+/* Threads per tile CTA: 128 for sparse tiles (nine CTAs per SM), 256 when
  * a tile may hold more agents than half its cells (its shared memory then
  * limits the SM to about four CTAs). */
 constexpr int NT_SPARSE = 128, NT_DENSE = 256;
+/* Resident CTAs per SM the register allocation is bounded for: 56
+ * registers a thread for 128-thread CTAs (nine per SM; 48 registers, ten
+ * per SM, spill and run slower), 64 for 256-thread ones. */
+#define CTAS_PER_SM(nt) ((nt) == NT_SPARSE ? 9 : 4)
 constexpr uint32_t NCLS = 32;          /* group classes of a tile (one per lane) */
 constexpr uint32_t CLS_FOREIGN = 30;   /* classes 0..29: other destination tiles */
 constexpr uint32_t CLS_OWN = 30;       /* moved within the tile                  */
@@ -628,7 +632,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
  * host sizes the grid from it and moves it when runs are admitted or
  * retired), so a serving world's free tile space costs nothing. */
 template <int CPT, int NT>
-__global__ void __launch_bounds__(NT, 1024 / NT) k_step_act(WorldDev w)
+__global__ void __launch_bounds__(NT, CTAS_PER_SM(NT)) k_step_act(WorldDev w)
 {
 	extern __shared__ __align__(16) uint32_t sm[];
 	if (blockIdx.x >= min(w.ctr->tile_hi, w.n_tiles)) return;
@@ -638,7 +642,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_step_act(WorldDev w)
 /* The first move of a freshly initialised run: one CTA per tile of
  * [tile0, tile0 + gridDim.x). */
 template <int CPT, int NT>
-__global__ void __launch_bounds__(NT, 1024 / NT) k_step_first(WorldDev w,
+__global__ void __launch_bounds__(NT, CTAS_PER_SM(NT)) k_step_first(WorldDev w,
 	const uint32_t *__restrict__ kS, const uint32_t *__restrict__ vS,
 	uint32_t tile0, uint32_t out_base)
 {
