@@ -254,6 +254,13 @@ int pp_sim_dump(pp_sim *sim, int dump_type, const char *agents_path,
 
 int pp_sim_destroy(pp_sim *sim);
 
+/* Device buffers of destroyed simulations, batches and servers stay cached
+ * in the process (at most a quarter of a device's memory; environment
+ * variable PP_CACHE_BYTES sets the limit, 0 disables the cache) and serve
+ * the next creation on that device without driver allocations. This frees
+ * the cached buffers of `device` (-1: every device); *released = bytes. */
+int pp_release_cached_memory(int device, uint64_t *released);
+
 /* ------------------------------------------------------------------ */
 /* Kernel-level entry points (host buffers in and out, synchronous).   */
 /* Used to check each kernel alone against the oracle.                 */

@@ -153,6 +153,7 @@ ABI = {
                                      _P(PPStatistics)]),
     "pp_sim_io_bytes": (C.c_int, [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)]),
     "pp_sim_destroy": (C.c_int, [C.c_void_p]),
+    "pp_release_cached_memory": (C.c_int, [C.c_int, _P(C.c_uint64)]),
     "pp_sim_snapshot_save": (C.c_int, [C.c_void_p, C.c_char_p]),
     "pp_sim_params": (C.c_int, [C.c_void_p, _P(PPParameters)]),
     "pp_sim_focal": (C.c_int, [C.c_void_p, _P(PPFocal)]),
@@ -375,6 +376,15 @@ def run(params, seed=0, iters=None, **kw):
     iters = params.iters if iters is None else iters
     with Simulation(params, seed, **kw) as sim:
         return [sim.stats0()] + sim.step(iters)
+
+
+def release_cached_memory(device=-1):
+    """Free the device buffers kept by the process cache of destroyed
+    worlds (pp_release_cached_memory); returns the bytes released."""
+    n = C.c_uint64()
+    _check(lib().pp_release_cached_memory(device, C.byref(n)),
+           "pp_release_cached_memory")
+    return n.value
 
 
 def batch_run(runs, pool_factor=4, tile_cells=0, digit_bits=0, use_graph=True,

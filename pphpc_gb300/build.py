@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                   "-Xcompiler", "-Wall"]
 CU_SOURCES = ["pp_kernels.cu", "pp_radix.cu", "pp_world.cu", "pp_serve.cu",
-              "pp_noalloc.cu", "pp_fused.cu", "pp_tune.cu"]
+              "pp_noalloc.cu", "pp_fused.cu", "pp_tune.cu", "pp_alloc.cu"]
 C_SOURCES = ["pp_host.c"]
 HEADERS = ["pp_device.cuh", "pp_kernels.cuh", "pp_block.cuh", "pp_world.cuh",
            "pp_act.cuh"]

@@ -66,7 +66,10 @@ void World::free_all()
 	if (graph_) cudaGraphDestroy(graph_);
 	gexec_ = nullptr;
 	graph_ = nullptr;
-	for (void *p : allocs_) cudaFree(p);
+	/* the buffers go back to the process cache only once no work of this
+	 * world can still touch them */
+	if (s_) cudaStreamSynchronize(s_);
+	for (auto &a : allocs_) cached_free(device_, a.first, a.second);
 	allocs_.clear();
 	if (s_) cudaStreamDestroy(s_);
 	s_ = nullptr;
@@ -75,12 +78,13 @@ void World::free_all()
 int World::alloc(size_t bytes, void **p)
 {
 	if (bytes == 0) bytes = 16;
-	cudaError_t e = cudaMalloc(p, bytes);
+	size_t got = 0;
+	cudaError_t e = cached_malloc(device_, bytes, p, &got);
 	if (e != cudaSuccess) {
 		cudaGetLastError();
 		return e == cudaErrorMemoryAllocation ? PP_OUT_OF_RESOURCES : PP_ERR_CUDA;
 	}
-	allocs_.push_back(*p);
+	allocs_.emplace_back(*p, got);
 	bytes_ += bytes;
 	return PP_SUCCESS;
 }

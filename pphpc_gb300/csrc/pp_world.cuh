@@ -6,6 +6,7 @@
  */
 #pragma once
 
+#include <utility>
 #include <vector>
 #include <cstring>
 
@@ -31,6 +32,12 @@ struct RunSpec {
 		return init_val ? (uint64_t) init_n : (uint64_t) p.init_sheep + p.init_wolves;
 	}
 };
+
+/* Device buffers through the process-wide cache (pp_alloc.cu): *got is
+ * the size of the buffer handed out (at least bytes), to be passed back to
+ * cached_free. */
+cudaError_t cached_malloc(int device, size_t bytes, void **p, size_t *got);
+void cached_free(int device, void *p, size_t bytes);
 
 /* Energy field width for the reference's agent size (0, 32 or 64) on a
  * grid of p (32-bit agents hold 10-bit coordinates, pp_gpu.cl:236-316). */
@@ -117,7 +124,7 @@ private:
 	LaunchCfg lc_{};
 	std::vector<RunDev> runs_h_;
 	std::vector<uint16_t> tile_run_h_;
-	std::vector<void *> allocs_;
+	std::vector<std::pair<void *, size_t>> allocs_;
 	size_t bytes_ = 0;
 	uint32_t giter_ = 0;
 	uint32_t graph_iters_ = 0;

@@ -127,3 +127,19 @@ def test_sparse_tiles_bit_exact(side, version, seed, iters, pool, tile):
     # a pool of well under one agent per cell: the act runs 128-thread CTAs
     # (sparse tiles) instead of the 256-thread ones the other tests get
     _check_run(params(side, version), seed, iters, max_agents=pool, tile_cells=tile)
+
+
+def test_cached_device_buffers_reused_and_released():
+    """A destroyed world's buffers stay in the process cache; the next
+    world of the same shape reuses them, stale contents and all, with the
+    same results; releasing the cache frees them."""
+    pp.release_cached_memory()
+    p = params(200, 2, iters=60)
+    want = orc.run(p, 3)
+    first = rows_array(pp.run(p, 3))
+    cached = pp.release_cached_memory(0)
+    assert cached > 0 and pp.release_cached_memory(0) == 0
+    pp.run(p, 3)
+    again = rows_array(pp.run(p, 3))
+    assert first_diff(first, want) is None and first_diff(again, want) is None
+    assert pp.release_cached_memory() >= cached
