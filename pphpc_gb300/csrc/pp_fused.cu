@@ -222,8 +222,9 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 	 * c / CPT, so no two threads of a warp share a bank */
 #define SLOT(c) ((((c) % CPT) * NT) + (c) / CPT)
 	if (ACT) {
+		uint4 *z = reinterpret_cast<uint4 *>(scnt);
 #pragma unroll
-		for (int q = 0; q < CPT; q++) scnt[q * NT + tid] = 0;
+		for (int q = 0; q < CPT / 4; q++) z[q * NT + tid] = make_uint4(0u, 0u, 0u, 0u);
 	}
 
 	/* ---- inputs ---- */
