@@ -23,6 +23,7 @@
  * next act, so no act allocates with an atomic on a shared counter.
  */
 #include <algorithm>
+#include <type_traits>
 
 #include "pp_act.cuh"
 
@@ -267,15 +268,13 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		if (tid < 8) w.part[(size_t) tile * 8 + tid] = 0;
 		return;
 	}
-	uint32_t *UK, *UV, *PERM, *LK, *LV;
-	if (in_smem) {
-		UK = sk; UV = sv; PERM = sperm; LK = sp; LV = sd;
-	} else {
-		const uint32_t xb = s_xbase;
-		UK = w.scratch_prio + xb; UV = w.scratch_kid + xb;
-		PERM = w.scratch_perm + 3ull * xb;
-		LK = w.scratch_key + xb; LV = w.scratch_val + xb;
-	}
+	/* The phases, instantiated once for a tile whose arrays are in shared
+	 * memory and once for a crowded tile's global scratch: each copy then
+	 * addresses one memory space directly (shared loads and stores with
+	 * 32-bit addresses) instead of through generic pointers. */
+	auto phases = [&](auto smem_tag, uint32_t *UK, uint32_t *UV, uint32_t *PERM,
+		uint32_t *LK, uint32_t *LV) {
+	constexpr bool in_smem = decltype(smem_tag)::value;
 	uint32_t *LP = UK, *LD = UV;      /* priorities / dice, then offsets / kids */
 
 	uint32_t eats = 0;
@@ -626,6 +625,14 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 				w.part[(size_t) tile * 8 + tid] = sum;
 			}
 		}
+	}
+	};
+	if (in_smem) {
+		phases(std::true_type{}, sk, sv, sperm, sp, sd);
+	} else {
+		const uint32_t xb = s_xbase;
+		phases(std::false_type{}, w.scratch_prio + xb, w.scratch_kid + xb,
+			w.scratch_perm + 3ull * xb, w.scratch_key + xb, w.scratch_val + xb);
 	}
 }
 
