@@ -22,6 +22,8 @@ ours:       W untimed iterations, then K iterations timed with CUDA events
             iteration's start, P = 4 sort passes at this grid size; the
             8 bytes per birth are left out), attributed to the fused
             act+move kernel, which does the whole iteration but the stats.
+            `lower_bound` puts the algorithm-free 12 C + 32 N bytes per
+            iteration over the timed iterations.
             `batched` runs the 64-run mix (32 x 200^2 v1, 16 x 800^2 v2,
             8 x 1600^2 v1, 8 x 3200^2 v2, seeds 100..163, --batch-iters
             iterations each) once through pp_batch_run (one world, every
@@ -285,6 +287,10 @@ def run_ours(args, dist):
     step_bytes = sum(k[3] for k in kernels) / prof_iters
     step_ms = sum(k[2] for k in kernels) / prof_iters
     timed_spec_bytes = sum(spec_bytes_per_iter(cells, r.sheep + r.wolves)[0] for r in rows)
+    # algorithm-free lower bound: each cell's grass read and written and its
+    # cell offsets written and read once (12 B), each agent read and written
+    # once in and out (32 B)
+    timed_lb_bytes = sum(12.0 * cells + 32.0 * (r.sheep + r.wolves) for r in rows)
 
     # -- end to end through the C ABI with host buffers --
     dist.barrier()
@@ -327,6 +333,11 @@ def run_ours(args, dist):
                            "frac": timed_spec_bytes / (ms_max / 1e3) / 1e9 / peak,
                            "note": "same per-iteration figure over the K timed "
                                    "iterations and their whole device time"},
+        "lower_bound": {"bytes": timed_lb_bytes,
+                        "achieved_gbs": timed_lb_bytes / (ms_max / 1e3) / 1e9,
+                        "frac": timed_lb_bytes / (ms_max / 1e3) / 1e9 / peak,
+                        "note": "algorithm-free lower bound 12 C + 32 N per iteration "
+                                "over the K timed iterations"},
         "kernel_bytes": {"moved_bytes_per_step": step_bytes,
                          "kernel_ms_per_step": step_ms,
                          "achieved_gbs": step_bytes / (step_ms / 1e3) / 1e9,
