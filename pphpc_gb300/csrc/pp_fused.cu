@@ -274,209 +274,209 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 	 * 32-bit addresses) instead of through generic pointers. */
 	auto phases = [&](auto smem_tag, uint32_t *UK, uint32_t *UV, uint32_t *PERM,
 		uint32_t *LK, uint32_t *LV) {
-	constexpr bool in_smem = decltype(smem_tag)::value;
-	uint32_t *LP = UK, *LD = UV;      /* priorities / dice, then offsets / kids */
+		constexpr bool in_smem = decltype(smem_tag)::value;
+		uint32_t *LP = UK, *LD = UV;      /* priorities / dice, then offsets / kids */
 
-	uint32_t eats = 0;
-	if (!ACT) {
-		for (uint32_t j = tid; j < m; j += NT) {
-			LK[j] = kS[a0 + j] - c0;
-			LV[j] = vS[a0 + j];
-		}
-		__syncthreads();
-	} else {
-		/* gather the tile's groups and count agents per cell: item j comes
-		 * from the last group whose prefix is <= j (groups with equal
-		 * prefixes before it are empty), found by a binary search over
-		 * the lanes' group prefixes; two items in flight per thread */
-		const uint32_t *kGi = pin ? w.kG1 : w.kG0;
-		const uint32_t *vGi = pin ? w.vG1 : w.vG0;
-		const uint32_t m_up = (m + NT - 1) / NT * NT;   /* warp-uniform trip count */
-		for (uint32_t j0 = tid; j0 < m_up; j0 += 2 * NT) {
-			uint32_t src[2];
+		uint32_t eats = 0;
+		if (!ACT) {
+			for (uint32_t j = tid; j < m; j += NT) {
+				LK[j] = kS[a0 + j] - c0;
+				LV[j] = vS[a0 + j];
+			}
+			__syncthreads();
+		} else {
+			/* gather the tile's groups and count agents per cell: item j comes
+			 * from the last group whose prefix is <= j (groups with equal
+			 * prefixes before it are empty), found by a binary search over
+			 * the lanes' group prefixes; two items in flight per thread */
+			const uint32_t *kGi = pin ? w.kG1 : w.kG0;
+			const uint32_t *vGi = pin ? w.vG1 : w.vG0;
+			const uint32_t m_up = (m + NT - 1) / NT * NT;   /* warp-uniform trip count */
+			for (uint32_t j0 = tid; j0 < m_up; j0 += 2 * NT) {
+				uint32_t src[2];
 #pragma unroll
-			for (int u = 0; u < 2; u++) {
-				const uint32_t j = j0 + u * NT;
-				uint32_t lo = 0, hi = max(nin, 1u);     /* last q with pref <= j */
+				for (int u = 0; u < 2; u++) {
+					const uint32_t j = j0 + u * NT;
+					uint32_t lo = 0, hi = max(nin, 1u);     /* last q with pref <= j */
 #pragma unroll
-				for (int step = 0; step < 5; step++) {
-					const uint32_t mid = (lo + hi) >> 1;
-					const uint32_t pm = __shfl_sync(0xffffffffu, grp_pref, mid);
-					if (hi - lo > 1) {
-						if (pm <= j) lo = mid; else hi = mid;
+					for (int step = 0; step < 5; step++) {
+						const uint32_t mid = (lo + hi) >> 1;
+						const uint32_t pm = __shfl_sync(0xffffffffu, grp_pref, mid);
+						if (hi - lo > 1) {
+							if (pm <= j) lo = mid; else hi = mid;
+						}
+					}
+					src[u] = __shfl_sync(0xffffffffu, grp_start, lo)
+						+ (j - __shfl_sync(0xffffffffu, grp_pref, lo));
+				}
+				uint32_t kk[2], vv[2];
+#pragma unroll
+				for (int u = 0; u < 2; u++) {
+					if (j0 + u * NT < m) {
+						kk[u] = kGi[src[u]];
+						vv[u] = vGi[src[u]];
 					}
 				}
-				src[u] = __shfl_sync(0xffffffffu, grp_start, lo)
-					+ (j - __shfl_sync(0xffffffffu, grp_pref, lo));
-			}
-			uint32_t kk[2], vv[2];
 #pragma unroll
-			for (int u = 0; u < 2; u++) {
-				if (j0 + u * NT < m) {
-					kk[u] = kGi[src[u]];
-					vv[u] = vGi[src[u]];
+				for (int u = 0; u < 2; u++) {
+					const uint32_t j = j0 + u * NT;
+					if (j < m) {
+						UK[j] = kk[u];
+						UV[j] = vv[u];
+						atomicAdd(&scnt[SLOT(kk[u] & lcmask)], 1u);
+					}
 				}
 			}
+			__syncthreads();
+			if (tid == 0) w.inbox_n[(size_t) pin * w.n_tiles + tile] = 0;
+			{
+				uint32_t loc = 0;
 #pragma unroll
-			for (int u = 0; u < 2; u++) {
-				const uint32_t j = j0 + u * NT;
-				if (j < m) {
-					UK[j] = kk[u];
-					UV[j] = vv[u];
-					atomicAdd(&scnt[SLOT(kk[u] & lcmask)], 1u);
+				for (int q = 0; q < CPT; q++) {
+					loc += scnt[q * NT + tid];
+				}
+				uint32_t tot;
+				uint32_t run_start = step_excl_scan<NT>(loc, &tot);
+#pragma unroll
+				for (int q = 0; q < CPT; q++) {
+					const uint32_t c = scnt[q * NT + tid];
+					scnt[q * NT + tid] = run_start;
+					run_start += c;
 				}
 			}
-		}
-		__syncthreads();
-		if (tid == 0) w.inbox_n[(size_t) pin * w.n_tiles + tile] = 0;
-		{
-			uint32_t loc = 0;
-#pragma unroll
-			for (int q = 0; q < CPT; q++) {
-				loc += scnt[q * NT + tid];
+			__syncthreads();
+			for (uint32_t j = tid; j < m; j += NT)
+				PERM[atomicAdd(&scnt[SLOT(UK[j] & lcmask)], 1u)] = j;
+			__syncthreads();
+			/* scnt[SLOT(c)] is now the end of cell c, and cell c's agents
+			 * occupy [end of c - 1, end of c) in arrival order; each goes to
+			 * the cell's start plus its rank in canonical order, which only
+			 * an agent sharing its cell has to count. LK holds the cell in
+			 * bits 0-15 and the rank in the cell's list in bits 16-31. */
+			for (uint32_t i = tid; i < m; i += NT) {
+				const uint32_t j = PERM[i];
+				const uint32_t rk = UK[j], c = rk & lcmask;
+				const uint32_t e = scnt[SLOT(c)], b = c ? scnt[SLOT(c - 1)] : 0;
+				uint32_t d = i;
+				if (e - b > 1) {
+					const uint32_t lr = lt0 + c;
+					const uint32_t y = fastdiv_div(lr, run.gxdiv), x = lr - y * run.gx;
+					const int64_t kx = order_key(rk, x, y, run.gx, run.gy);
+					d = b;
+					for (uint32_t q = b; q < e; q++)
+						d += order_key(UK[PERM[q]], x, y, run.gx, run.gy) < kx;
+				}
+				if (d - b > 0xffffu) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
+				LK[d] = c | (d - b) << 16;
+				LV[d] = UV[j];
 			}
-			uint32_t tot;
-			uint32_t run_start = step_excl_scan<NT>(loc, &tot);
-#pragma unroll
-			for (int q = 0; q < CPT; q++) {
-				const uint32_t c = scnt[q * NT + tid];
-				scnt[q * NT + tid] = run_start;
-				run_start += c;
-			}
-		}
-		__syncthreads();
-		for (uint32_t j = tid; j < m; j += NT)
-			PERM[atomicAdd(&scnt[SLOT(UK[j] & lcmask)], 1u)] = j;
-		__syncthreads();
-		/* scnt[SLOT(c)] is now the end of cell c, and cell c's agents
-		 * occupy [end of c - 1, end of c) in arrival order; each goes to
-		 * the cell's start plus its rank in canonical order, which only
-		 * an agent sharing its cell has to count. LK holds the cell in
-		 * bits 0-15 and the rank in the cell's list in bits 16-31. */
-		for (uint32_t i = tid; i < m; i += NT) {
-			const uint32_t j = PERM[i];
-			const uint32_t rk = UK[j], c = rk & lcmask;
-			const uint32_t e = scnt[SLOT(c)], b = c ? scnt[SLOT(c - 1)] : 0;
-			uint32_t d = i;
-			if (e - b > 1) {
-				const uint32_t lr = lt0 + c;
-				const uint32_t y = fastdiv_div(lr, run.gxdiv), x = lr - y * run.gx;
-				const int64_t kx = order_key(rk, x, y, run.gx, run.gy);
-				d = b;
-				for (uint32_t q = b; q < e; q++)
-					d += order_key(UK[PERM[q]], x, y, run.gx, run.gy) < kx;
-			}
-			if (d - b > 0xffffu) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
-			LK[d] = c | (d - b) << 16;
-			LV[d] = UV[j];
-		}
 #undef SLOT
-		__syncthreads();
-		/* B: draws of every agent */
-		for (uint32_t j = tid; j < m; j += NT) {
-			const uint32_t lk = LK[j], lc = lk & 0xffffu;
-			u4 r = rng(seed_lo, seed_hi, lt0 + lc, t, STREAM_ACT, lk >> 16);
-			LP[j] = r.x;
-			LD[j] = draw(r.y, 100);
-		}
-		cp_async_wait_all();
-		__syncthreads();
-		/* C: actions, one thread per agent */
-		ActParams ap;
-		ap.sheep_gain = run.sheep_gain; ap.sheep_thr = run.sheep_thr;
-		ap.sheep_prob = run.sheep_prob; ap.wolves_gain = run.wolves_gain;
-		ap.wolves_thr = run.wolves_thr; ap.wolves_prob = run.wolves_prob;
-		ap.restart = run.restart;
-		ap.emask = run.emask;
-		const uint16_t t16 = (uint16_t) t;
-		for (uint32_t j = tid; j < m; j += NT) {
-			const uint32_t lk = LK[j], lc = lk & 0xffffu;
-			const uint32_t p = j - (lk >> 16);
-			uint32_t e = j + 1;
-			while (e < m && (LK[e] >> 16) != 0) e++;
-			const int32_t dd = (int16_t) (uint16_t) (sgrass[lc] - t16);
-			uint32_t kid;
-			if (act_agent(j, p, e, LV, LP, ap, dd > 0 ? (uint32_t) dd : 0u, LD[j], &kid)) {
-				w.grass[c0 + lc] = (uint16_t) (t16 + (uint16_t) ap.restart);
-				eats++;
+			__syncthreads();
+			/* B: draws of every agent */
+			for (uint32_t j = tid; j < m; j += NT) {
+				const uint32_t lk = LK[j], lc = lk & 0xffffu;
+				u4 r = rng(seed_lo, seed_hi, lt0 + lc, t, STREAM_ACT, lk >> 16);
+				LP[j] = r.x;
+				LD[j] = draw(r.y, 100);
 			}
-			LD[j] = kid;
+			cp_async_wait_all();
+			__syncthreads();
+			/* C: actions, one thread per agent */
+			ActParams ap;
+			ap.sheep_gain = run.sheep_gain; ap.sheep_thr = run.sheep_thr;
+			ap.sheep_prob = run.sheep_prob; ap.wolves_gain = run.wolves_gain;
+			ap.wolves_thr = run.wolves_thr; ap.wolves_prob = run.wolves_prob;
+			ap.restart = run.restart;
+			ap.emask = run.emask;
+			const uint16_t t16 = (uint16_t) t;
+			for (uint32_t j = tid; j < m; j += NT) {
+				const uint32_t lk = LK[j], lc = lk & 0xffffu;
+				const uint32_t p = j - (lk >> 16);
+				uint32_t e = j + 1;
+				while (e < m && (LK[e] >> 16) != 0) e++;
+				const int32_t dd = (int16_t) (uint16_t) (sgrass[lc] - t16);
+				uint32_t kid;
+				if (act_agent(j, p, e, LV, LP, ap, dd > 0 ? (uint32_t) dd : 0u, LD[j], &kid)) {
+					w.grass[c0 + lc] = (uint16_t) (t16 + (uint16_t) ap.restart);
+					eats++;
+				}
+				LD[j] = kid;
+			}
+			__syncthreads();
 		}
-		__syncthreads();
-	}
 
-	/* ---- E0: output offsets (each survivor, then its newborn), stats,
-	 * and the output -> agent map OUTJ (agent index | newborn << 15) ---- */
-	const uint32_t ch = (m + NT - 1) / NT;
-	const uint32_t ja = min(tid * ch, m), jb = min(ja + ch, m);
-	uint32_t cnt = 0, sheep = 0, wolves = 0;
-	uint64_t sen = 0, wen = 0;
-	if (ACT) {
-		for (uint32_t j = ja; j < jb; j++) {
-			const uint32_t v = LV[j], kd = LD[j];
-			const uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
-			if (!(v & EATEN_BIT)) {
-				cnt++;
-				if (tb) { wolves++; wen += en; } else { sheep++; sen += en; }
-			}
-			if (kd) {
-				cnt++;
-				if (tb) { wolves++; wen += kd; } else { sheep++; sen += kd; }
-			}
-		}
-	}
-	uint32_t total = m;
-	/* output map: 16-bit entries in the permutation's shared array (2 m
-	 * <= 2 act_cap), 32-bit ones in a crowded tile's scratch; directions:
-	 * bytes in the cell counters (2 m <= 4 T) or after the map */
-	uint16_t *OUTJ16 = reinterpret_cast<uint16_t *>(PERM);
-	uint32_t *OUTJ32 = PERM;
-	uint8_t *DIR = in_smem ? reinterpret_cast<uint8_t *>(scnt)
-		: reinterpret_cast<uint8_t *>(PERM + 2 * m);
-	if (ACT) {
-		uint32_t o = step_excl_scan<NT>(cnt, &total);
-		for (uint32_t j = ja; j < jb; j++) {
-			LP[j] = o;
-			if (!(LV[j] & EATEN_BIT)) {
-				if (in_smem) OUTJ16[o] = (uint16_t) j; else OUTJ32[o] = j;
-				o++;
-			}
-			if (LD[j]) {
-				if (in_smem) OUTJ16[o] = (uint16_t) (j | 0x8000u);
-				else OUTJ32[o] = j | 0x80000000u;
-				o++;
-			}
-		}
-		__syncthreads();
-	}
-	/* the tile's slots in the group buffer: twice its dense input base
-	 * (at most two outputs per input), or after out_base for a first move */
-	const uint32_t gb = ACT ? 2 * dbase_t : out_base + a0;
-
-	/* output o: its agent j, whether it is a newborn, its energy and rank
-	 * in its cell's new list */
-	auto output = [&](uint32_t o, uint32_t &j, uint32_t &nb, uint32_t &en,
-		uint32_t &rank) {
+		/* ---- E0: output offsets (each survivor, then its newborn), stats,
+		 * and the output -> agent map OUTJ (agent index | newborn << 15) ---- */
+		const uint32_t ch = (m + NT - 1) / NT;
+		const uint32_t ja = min(tid * ch, m), jb = min(ja + ch, m);
+		uint32_t cnt = 0, sheep = 0, wolves = 0;
+		uint64_t sen = 0, wen = 0;
 		if (ACT) {
-			if (in_smem) {
-				const uint32_t u = OUTJ16[o];
-				j = u & 0x7fffu;
-				nb = u >> 15;
-			} else {
-				const uint32_t u = OUTJ32[o];
-				j = u & 0x7fffffffu;
-				nb = u >> 31;
+			for (uint32_t j = ja; j < jb; j++) {
+				const uint32_t v = LV[j], kd = LD[j];
+				const uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
+				if (!(v & EATEN_BIT)) {
+					cnt++;
+					if (tb) { wolves++; wen += en; } else { sheep++; sen += en; }
+				}
+				if (kd) {
+					cnt++;
+					if (tb) { wolves++; wen += kd; } else { sheep++; sen += kd; }
+				}
 			}
-		} else {
-			j = o;
-			nb = 0;
 		}
-		const uint32_t lk = LK[j];
-		uint32_t f = j - (lk >> 16);
-		if (!ACT)
-			while (f > 0 && LK[f - 1] == lk) f--;
-		rank = o - (ACT ? LP[f] : f);
-		en = nb ? LD[j] : (LV[j] & ENERGY_MASK);
+		uint32_t total = m;
+		/* output map: 16-bit entries in the permutation's shared array (2 m
+		 * <= 2 act_cap), 32-bit ones in a crowded tile's scratch; directions:
+		 * bytes in the cell counters (2 m <= 4 T) or after the map */
+		uint16_t *OUTJ16 = reinterpret_cast<uint16_t *>(PERM);
+		uint32_t *OUTJ32 = PERM;
+		uint8_t *DIR = in_smem ? reinterpret_cast<uint8_t *>(scnt)
+			: reinterpret_cast<uint8_t *>(PERM + 2 * m);
+		if (ACT) {
+			uint32_t o = step_excl_scan<NT>(cnt, &total);
+			for (uint32_t j = ja; j < jb; j++) {
+				LP[j] = o;
+				if (!(LV[j] & EATEN_BIT)) {
+					if (in_smem) OUTJ16[o] = (uint16_t) j; else OUTJ32[o] = j;
+					o++;
+				}
+				if (LD[j]) {
+					if (in_smem) OUTJ16[o] = (uint16_t) (j | 0x8000u);
+					else OUTJ32[o] = j | 0x80000000u;
+					o++;
+				}
+			}
+			__syncthreads();
+		}
+		/* the tile's slots in the group buffer: twice its dense input base
+		 * (at most two outputs per input), or after out_base for a first move */
+		const uint32_t gb = ACT ? 2 * dbase_t : out_base + a0;
+
+		/* output o: its agent j, whether it is a newborn, its energy and rank
+		 * in its cell's new list */
+		auto output = [&](uint32_t o, uint32_t &j, uint32_t &nb, uint32_t &en,
+			uint32_t &rank) {
+			if (ACT) {
+				if (in_smem) {
+					const uint32_t u = OUTJ16[o];
+					j = u & 0x7fffu;
+					nb = u >> 15;
+				} else {
+					const uint32_t u = OUTJ32[o];
+					j = u & 0x7fffffffu;
+					nb = u >> 31;
+				}
+			} else {
+				j = o;
+				nb = 0;
+			}
+			const uint32_t lk = LK[j];
+			uint32_t f = j - (lk >> 16);
+			if (!ACT)
+				while (f > 0 && LK[f - 1] == lk) f--;
+			rank = o - (ACT ? LP[f] : f);
+			en = nb ? LD[j] : (LV[j] & ENERGY_MASK);
 	};
 
 	/* ---- E1: move draws of the outputs, per-class counts; with room in
