@@ -25,6 +25,8 @@
  * an array position. Every kernel reads its sizes from device memory, so an
  * iteration is a fixed launch sequence, captured once as a CUDA graph.
  */
+#include <type_traits>
+
 #include "pp_kernels.cuh"
 #include "pp_block.cuh"
 #include "pp_act.cuh"
@@ -269,7 +271,7 @@ __global__ void __launch_bounds__(ACT_THREADS, 5) k_act(WorldDev w,
 		return;
 	}
 	const uint32_t seed_lo = run.seed_lo, seed_hi = run.seed_hi;
-	const uint32_t cbase = run.cbase, ncells = run.ncells;
+	const uint32_t cbase = run.cbase;
 	ActParams ap;
 	ap.sheep_gain = run.sheep_gain; ap.sheep_thr = run.sheep_thr;
 	ap.sheep_prob = run.sheep_prob; ap.wolves_gain = run.wolves_gain;
@@ -282,174 +284,172 @@ __global__ void __launch_bounds__(ACT_THREADS, 5) k_act(WorldDev w,
 	const uint32_t m = a1 - a0;
 	const bool in_smem = m <= w.act_cap;
 	/* The sort grouped agents by tile only, in canonical order (source
-	 * cell, source rank); group them by cell here, keeping that order. */
-	uint32_t *UK, *UV, *PERM, *LK, *LV, *LP, *LD;
-	if (in_smem) {
-		UK = sk; UV = sv; PERM = sperm; LK = sp; LV = sd; LP = sk; LD = sv;
-		for (uint32_t j = tid; j < m; j += ACT_THREADS) {
-			sk[j] = kS[a0 + j];
-			sv[j] = vS[a0 + j];
-		}
-	} else {
-		UK = const_cast<uint32_t *>(kS) + a0; UV = vS + a0;
-		PERM = w.scratch_perm + a0;
-		LK = w.scratch_key + a0; LV = w.scratch_val + a0;
-		LP = w.scratch_prio + a0; LD = w.scratch_kid + a0;
-	}
-	const uint32_t cell0 = tid * CPT;
-	/* per-cell counters, transposed like the countdowns: cell c lives at
-	 * SLOT(c) = (c % CPT) * 256 + c / CPT, so no two threads of a warp
-	 * share a bank */
-#define SLOT(c) ((((c) % CPT) * ACT_THREADS) + (c) / CPT)
-#pragma unroll
-	for (int q = 0; q < CPT; q++) scnt[q * ACT_THREADS + tid] = 0;
-	__syncthreads();
-	/* counting sort of the tile's agents by cell */
-	uint32_t multi = 0;   /* this thread's cells holding two or more agents */
-	for (uint32_t j = tid; j < m; j += ACT_THREADS) {
-		const uint32_t lc = UK[j] - c0;
-		atomicAdd(&scnt[SLOT(lc)], 1u);
-	}
-	__syncthreads();
-	{
-		uint32_t loc = 0;
-#pragma unroll
-		for (int q = 0; q < CPT; q++) {
-			const uint32_t c = scnt[q * ACT_THREADS + tid];
-			loc += c;
-			if (c > 1) multi |= 1u << q;
-		}
-		uint32_t tot;
-		uint32_t run_start = block_excl_scan(loc, &tot);
-#pragma unroll
-		for (int q = 0; q < CPT; q++) {
-			uint32_t c = scnt[q * ACT_THREADS + tid];
-			scnt[q * ACT_THREADS + tid] = run_start;
-			run_start += c;
-		}
-	}
-	__syncthreads();
-	for (uint32_t j = tid; j < m; j += ACT_THREADS) {
-		const uint32_t lc = UK[j] - c0;
-		PERM[atomicAdd(&scnt[SLOT(lc)], 1u)] = j;
-	}
-	__syncthreads();
-	/* scnt[SLOT(c)] is now the end of cell c; restore the arrival order of
-	 * each cell's list (only cells holding two or more agents) */
-	while (multi) {
-		const int q = __ffs(multi) - 1;
-		multi &= multi - 1;
-		const uint32_t c = cell0 + q;
-		const uint32_t b = c ? scnt[SLOT(c - 1)] : 0, e = scnt[SLOT(c)];
-		for (uint32_t i = b + 1; i < e; i++) {
-			const uint32_t x = PERM[i];
-			uint32_t h = i;
-			while (h > b && PERM[h - 1] > x) { PERM[h] = PERM[h - 1]; h--; }
-			PERM[h] = x;
-		}
-	}
-#undef SLOT
-	__syncthreads();
-	for (uint32_t i = tid; i < m; i += ACT_THREADS) {
-		const uint32_t j = PERM[i];
-		LK[i] = UK[j] - c0;
-		LV[i] = UV[j];
-	}
-	__syncthreads();
-	/* B: draws of every agent, and its cell's countdown max(0, regrowth -
-	 * t) read before any sheep eats (LD = dice | countdown << 7) */
-	const uint16_t t16 = (uint16_t) t;
-	for (uint32_t j = tid; j < m; j += ACT_THREADS) {
-		const uint32_t lc = LK[j];
-		uint32_t k = 0;
-		while (k < j && LK[j - k - 1] == lc) k++;
-		u4 r = rng(seed_lo, seed_hi, lt0 + lc, t, STREAM_ACT, k);
-		const int32_t dd = (int16_t) (uint16_t) (w.grass[c0 + lc] - t16);
-		LP[j] = r.x;
-		LD[j] = draw(r.y, 100) | (dd > 0 ? (uint32_t) dd << 7 : 0u);
-	}
-	__syncthreads();
-	/* C: actions, one thread per agent; a sheep that eats sets its cell's
-	 * regrowth to t + restart, counted for the run's regrowth histogram */
-	uint32_t eats = 0;
-	for (uint32_t j = tid; j < m; j += ACT_THREADS) {
-		const uint32_t lc = LK[j];
-		uint32_t p = j, e = j + 1;
-		while (p > 0 && LK[p - 1] == lc) p--;
-		while (e < m && LK[e] == lc) e++;
-		const uint32_t dg = LD[j];
-		uint32_t kid;
-		if (act_agent(j, p, e, LV, LP, ap, dg >> 7, dg & 127u, &kid)) {
-			w.grass[c0 + lc] = (uint16_t) (t16 + (uint16_t) ap.restart);
-			eats++;
-		}
-		LD[j] = kid;
-	}
-	__syncthreads();
-	/* E: outputs in list order, contiguous agent chunks per thread */
-	const uint32_t ch = (m + ACT_THREADS - 1) / ACT_THREADS;
-	const uint32_t ja = min(tid * ch, m), jb = min(ja + ch, m);
-	uint32_t cnt = 0;
-	for (uint32_t j = ja; j < jb; j++)
-		cnt += ((LV[j] & EATEN_BIT) == 0) + (LD[j] != 0);
-	uint32_t total;
-	const uint32_t excl = block_excl_scan(cnt, &total);
-	const uint32_t rs = 2 * a0;
-	if (tid == 0) {
-		w.rstart[tile] = rs;
-		w.rcnt[tile] = total;
-	}
-	uint32_t o = rs + excl;
-	uint32_t sheep = 0, wolves = 0;
-	uint64_t sen = 0, wen = 0;
-	for (uint32_t j = ja; j < jb; j++) {
-		const uint32_t v = LV[j], k = LK[j] + c0, kd = LD[j];
-		const uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
-		if (!(v & EATEN_BIT)) {
-			w.kR[o] = k;
-			w.vR[o] = v;
-			o++;
-			if (tb) { wolves++; wen += en; }
-			else { sheep++; sen += en; }
-		}
-		if (kd) {
-			w.kR[o] = k;
-			w.vR[o] = tb | kd;
-			o++;
-			if (tb) { wolves++; wen += kd; }
-			else { sheep++; sen += kd; }
-		}
-	}
-	/* per-tile partial stats; the tile's eating events go to the run's
-	 * regrowth histogram slot of iteration t + restart */
-	{
-		__shared__ uint64_t red[5][ACT_THREADS / 32];
-		const uint32_t lane = tid & 31, wid = tid >> 5;
-		const uint32_t sw = warp_sum(sheep | (wolves << 16));
-		const uint32_t ew = warp_sum(eats);
-		const uint64_t se = warp_sum(sen), we = warp_sum(wen);
-		if (lane == 0) {
-			red[0][wid] = sw & 0xffffu;
-			red[1][wid] = sw >> 16;
-			red[2][wid] = ew;
-			red[3][wid] = se;
-			red[4][wid] = we;
-		}
-		__syncthreads();
-		if (tid < 5) {
-			uint64_t sum = 0;
-			for (uint32_t q = 0; q < ACT_THREADS / 32; q++) sum += red[tid][q];
-			if (tid == 2) {
-				if (sum)
-					atomicAdd(&w.fring[run.fbase + (t + ap.restart) % (ap.restart + 1)],
-						(uint32_t) sum);
-				w.part[(size_t) tile * 8 + 2] = 0;
-				w.part[(size_t) tile * 8 + 5] = 0;
-			} else {
-				w.part[(size_t) tile * 8 + tid] = sum;
+	 * cell, source rank); group them by cell here, keeping that order.
+	 * The phases are instantiated once for a tile whose arrays are in
+	 * shared memory and once for a crowded tile's global arrays, so each
+	 * copy addresses one memory space directly. */
+	auto phases = [&](auto smem_tag, uint32_t *UK, uint32_t *UV, uint32_t *PERM,
+		uint32_t *LK, uint32_t *LV, uint32_t *LP, uint32_t *LD) {
+		constexpr bool SMEM = decltype(smem_tag)::value;
+		if (SMEM) {
+			for (uint32_t j = tid; j < m; j += ACT_THREADS) {
+				UK[j] = kS[a0 + j];
+				UV[j] = vS[a0 + j];
 			}
 		}
-	}
+		/* per-cell counters, transposed like the countdowns: cell c lives at
+		 * SLOT(c) = (c % CPT) * 256 + c / CPT, so no two threads of a warp
+		 * share a bank */
+#define SLOT(c) ((((c) % CPT) * ACT_THREADS) + (c) / CPT)
+#pragma unroll
+		for (int q = 0; q < CPT; q++) scnt[q * ACT_THREADS + tid] = 0;
+		__syncthreads();
+		/* counting sort of the tile's agents by cell */
+		for (uint32_t j = tid; j < m; j += ACT_THREADS) {
+			const uint32_t lc = UK[j] - c0;
+			atomicAdd(&scnt[SLOT(lc)], 1u);
+		}
+		__syncthreads();
+		{
+			uint32_t loc = 0;
+#pragma unroll
+			for (int q = 0; q < CPT; q++) {
+				loc += scnt[q * ACT_THREADS + tid];
+			}
+			uint32_t tot;
+			uint32_t run_start = block_excl_scan(loc, &tot);
+#pragma unroll
+			for (int q = 0; q < CPT; q++) {
+				uint32_t c = scnt[q * ACT_THREADS + tid];
+				scnt[q * ACT_THREADS + tid] = run_start;
+				run_start += c;
+			}
+		}
+		__syncthreads();
+		for (uint32_t j = tid; j < m; j += ACT_THREADS) {
+			const uint32_t lc = UK[j] - c0;
+			PERM[atomicAdd(&scnt[SLOT(lc)], 1u)] = j;
+		}
+		__syncthreads();
+		/* scnt[SLOT(c)] is now the end of cell c, whose agents occupy [end of
+		 * c - 1, end of c) in the order of the atomics; each goes to the cell's
+		 * start plus its rank in arrival order, which only an agent sharing
+		 * its cell has to count. LK holds the cell in bits 0-15 and the rank
+		 * in the cell's list in bits 16-31. */
+		for (uint32_t i = tid; i < m; i += ACT_THREADS) {
+			const uint32_t j = PERM[i];
+			const uint32_t lc = UK[j] - c0;
+			const uint32_t e = scnt[SLOT(lc)], b = lc ? scnt[SLOT(lc - 1)] : 0;
+			uint32_t d = i;
+			if (e - b > 1) {
+				d = b;
+				for (uint32_t q = b; q < e; q++) d += PERM[q] < j;
+			}
+			if (d - b > 0xffffu) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
+			LK[d] = lc | (d - b) << 16;
+			LV[d] = UV[j];
+		}
+#undef SLOT
+		__syncthreads();
+		/* B: draws of every agent, and its cell's countdown max(0, regrowth -
+		 * t) read before any sheep eats (LD = dice | countdown << 7) */
+		const uint16_t t16 = (uint16_t) t;
+		for (uint32_t j = tid; j < m; j += ACT_THREADS) {
+			const uint32_t lk = LK[j], lc = lk & 0xffffu;
+			u4 r = rng(seed_lo, seed_hi, lt0 + lc, t, STREAM_ACT, lk >> 16);
+			const int32_t dd = (int16_t) (uint16_t) (w.grass[c0 + lc] - t16);
+			LP[j] = r.x;
+			LD[j] = draw(r.y, 100) | (dd > 0 ? (uint32_t) dd << 7 : 0u);
+		}
+		__syncthreads();
+		/* C: actions, one thread per agent; a sheep that eats sets its cell's
+		 * regrowth to t + restart, counted for the run's regrowth histogram */
+		uint32_t eats = 0;
+		for (uint32_t j = tid; j < m; j += ACT_THREADS) {
+			const uint32_t lk = LK[j], lc = lk & 0xffffu;
+			const uint32_t p = j - (lk >> 16);
+			uint32_t e = j + 1;
+			while (e < m && (LK[e] >> 16) != 0) e++;
+			const uint32_t dg = LD[j];
+			uint32_t kid;
+			if (act_agent(j, p, e, LV, LP, ap, dg >> 7, dg & 127u, &kid)) {
+				w.grass[c0 + lc] = (uint16_t) (t16 + (uint16_t) ap.restart);
+				eats++;
+			}
+			LD[j] = kid;
+		}
+		__syncthreads();
+		/* E: outputs in list order, contiguous agent chunks per thread */
+		const uint32_t ch = (m + ACT_THREADS - 1) / ACT_THREADS;
+		const uint32_t ja = min(tid * ch, m), jb = min(ja + ch, m);
+		uint32_t cnt = 0;
+		for (uint32_t j = ja; j < jb; j++)
+			cnt += ((LV[j] & EATEN_BIT) == 0) + (LD[j] != 0);
+		uint32_t total;
+		const uint32_t excl = block_excl_scan(cnt, &total);
+		const uint32_t rs = 2 * a0;
+		if (tid == 0) {
+			w.rstart[tile] = rs;
+			w.rcnt[tile] = total;
+		}
+		uint32_t o = rs + excl;
+		uint32_t sheep = 0, wolves = 0;
+		uint64_t sen = 0, wen = 0;
+		for (uint32_t j = ja; j < jb; j++) {
+			const uint32_t v = LV[j], k = (LK[j] & 0xffffu) + c0, kd = LD[j];
+			const uint32_t tb = v & TYPE_BIT, en = v & ENERGY_MASK;
+			if (!(v & EATEN_BIT)) {
+				w.kR[o] = k;
+				w.vR[o] = v;
+				o++;
+				if (tb) { wolves++; wen += en; }
+				else { sheep++; sen += en; }
+			}
+			if (kd) {
+				w.kR[o] = k;
+				w.vR[o] = tb | kd;
+				o++;
+				if (tb) { wolves++; wen += kd; }
+				else { sheep++; sen += kd; }
+			}
+		}
+		/* per-tile partial stats; the tile's eating events go to the run's
+		 * regrowth histogram slot of iteration t + restart */
+		{
+			__shared__ uint64_t red[5][ACT_THREADS / 32];
+			const uint32_t lane = tid & 31, wid = tid >> 5;
+			const uint32_t sw = warp_sum(sheep | (wolves << 16));
+			const uint32_t ew = warp_sum(eats);
+			const uint64_t se = warp_sum(sen), we = warp_sum(wen);
+			if (lane == 0) {
+				red[0][wid] = sw & 0xffffu;
+				red[1][wid] = sw >> 16;
+				red[2][wid] = ew;
+				red[3][wid] = se;
+				red[4][wid] = we;
+			}
+			__syncthreads();
+			if (tid < 5) {
+				uint64_t sum = 0;
+				for (uint32_t q = 0; q < ACT_THREADS / 32; q++) sum += red[tid][q];
+				if (tid == 2) {
+					if (sum)
+						atomicAdd(&w.fring[run.fbase + (t + ap.restart) % (ap.restart + 1)],
+							(uint32_t) sum);
+					w.part[(size_t) tile * 8 + 2] = 0;
+					w.part[(size_t) tile * 8 + 5] = 0;
+				} else {
+					w.part[(size_t) tile * 8 + tid] = sum;
+				}
+			}
+		}
+	};
+	if (in_smem)
+		phases(std::true_type{}, sk, sv, sperm, sp, sd, sk, sv);
+	else
+		phases(std::false_type{}, const_cast<uint32_t *>(kS) + a0, vS + a0,
+			w.scratch_perm + a0, w.scratch_key + a0, w.scratch_val + a0,
+			w.scratch_prio + a0, w.scratch_kid + a0);
 }
 
 /* Per chunk of tiles (chunks taken by ticket, so a chunk's predecessors are
