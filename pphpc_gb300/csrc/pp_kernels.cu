@@ -549,8 +549,17 @@ __global__ void __launch_bounds__(256) k_finish(WorldDev w)
 	};
 	const uint32_t tpt = (per + blockDim.x - 1) / blockDim.x;
 	const uint32_t ta = min(t0 + threadIdx.x * tpt, t1), tb = min(ta + tpt, t1);
+	/* a thread's first tiles keep their counts in registers for the base
+	 * writes below */
+	constexpr uint32_t KEEP = 4;
+	uint32_t kept[KEEP];
 	uint32_t local = 0;
-	for (uint32_t tl = ta; tl < tb; tl++) local += tile_count(tl);
+#pragma unroll
+	for (uint32_t q = 0; q < KEEP; q++) {
+		kept[q] = ta + q < tb ? tile_count(ta + q) : 0u;
+		local += kept[q];
+	}
+	for (uint32_t tl = ta + KEEP; tl < tb; tl++) local += tile_count(tl);
 	if (FUSED) {
 		/* the agent count after the act: all records, summed per CTA */
 		const uint32_t a = warp_sum(all);
@@ -564,7 +573,12 @@ __global__ void __launch_bounds__(256) k_finish(WorldDev w)
 	}
 	__syncthreads();
 	uint32_t run = s_base + excl;
-	for (uint32_t tl = ta; tl < tb; tl++) {
+#pragma unroll
+	for (uint32_t q = 0; q < KEEP; q++) {
+		if (ta + q < tb) w.dbase[ta + q] = run;
+		run += kept[q];
+	}
+	for (uint32_t tl = ta + KEEP; tl < tb; tl++) {
 		w.dbase[tl] = run;
 		run += tile_count(tl);
 	}
