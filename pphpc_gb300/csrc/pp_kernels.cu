@@ -69,6 +69,10 @@ __global__ void __launch_bounds__(256) k_regions(WorldDev w, uint32_t *ko,
 		for (uint32_t j0 = 0; j0 < cnt; j0 += 32) {
 			const uint32_t j = j0 + lane;
 			const bool valid = j < cnt;
+			/* past an overflow of the pool (its error is already raised)
+			 * the dense positions run beyond it: nothing is written there
+			 * and nothing counted */
+			const bool keep = valid && db + j < w.cap;
 			const uint32_t key = valid ? w.kR[rs + j] : 0xffffffffu;
 			const uint32_t val = valid ? w.vR[rs + j] : 0;
 			uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
@@ -80,14 +84,14 @@ __global__ void __launch_bounds__(256) k_regions(WorldDev w, uint32_t *ko,
 			carry_key = __shfl_sync(0xffffffffu, key, last);
 			carry_rank = __shfl_sync(0xffffffffu, k, last);
 			if (!MOVE) {
-				if (valid) {
+				if (keep) {
 					ko[db + j] = key;
 					vo[db + j] = val;
 				}
 				continue;
 			}
 			uint32_t nk = 0xffffffffu, nv = 0;
-			if (valid) {
+			if (keep) {
 				if (live) move_one(run, key, val, k, t, w.dead_key, nk, nv);
 				else { nk = w.dead_key; nv = val & TYPE_BIT; }
 				w.kB[db + j] = nk;
@@ -96,14 +100,14 @@ __global__ void __launch_bounds__(256) k_regions(WorldDev w, uint32_t *ko,
 			/* Digit counts: one atomic per warp when the warp's digits
 			 * agree (the high digits of a nearly cell-sorted array), else
 			 * one per lane. */
-			const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+			const uint32_t vmask = __ballot_sync(0xffffffffu, keep);
 			for (uint32_t p = 0; p < P; p++) {
 				uint32_t dig = (nk >> (w.sort_shift + p * d)) & mask;
 				uint32_t d0 = __shfl_sync(0xffffffffu, dig, 0);
-				bool same = __all_sync(0xffffffffu, !valid || dig == d0);
+				bool same = __all_sync(0xffffffffu, !keep || dig == d0);
 				if (same) {
 					if (lane == 0) atomicAdd(&sh_hist[(p << d) + d0], __popc(vmask));
-				} else if (valid) {
+				} else if (keep) {
 					atomicAdd(&sh_hist[(p << d) + dig], 1u);
 				}
 			}
