@@ -115,7 +115,8 @@ typedef struct pp_sim pp_sim;
 typedef struct pp_opts {
 	int device;             /* CUDA device ordinal (default 0)                */
 	uint32_t max_agents;    /* agent pool slots; 0 = 4 x initial agents, >= 1024 */
-	uint32_t tile_cells;    /* cells per act tile (power of 2); 0 = autotune  */
+	uint32_t tile_cells;    /* cells per act tile: 1024..8192, or 512 for the
+	                           fused pipeline; 0 = choose (or autotune)    */
 	uint32_t sort_digit_bits; /* radix digit width 4..8; 0 = autotune         */
 	uint32_t use_graph;     /* capture each iteration as a CUDA graph (1) or not (0) */
 	uint32_t sort_pipeline; /* 1 = per-iteration sort pipeline (move, LSD radix
@@ -414,8 +415,9 @@ typedef struct pp_tuning {
 	float ns_per_agent_step;    /* measured device cost of the winner      */
 } pp_tuning;
 
-/* Measure the candidate geometries (fused and sort pipelines, 1024..8192
- * cells per tile) on a sample of the workload -- the same parameters on at
+/* Measure the candidate geometries (fused pipeline on tiles of 512..8192
+ * cells, sort pipeline on 1024..8192) on a sample of the workload -- the
+ * same parameters on at
  * most 4096 x 4096 cells with agents and pool scaled by area -- and return
  * the one with the lowest device time per agent-step. Results are cached
  * per device and workload shape (and in the file named by PP_TUNE_CACHE,

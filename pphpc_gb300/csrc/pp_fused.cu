@@ -36,9 +36,10 @@ namespace {
 
 static_assert(IBX == 32, "the inbox is read by one warp");
 
-/* Threads per tile CTA: 128 for sparse tiles (nine CTAs per SM), 256 when
- * a tile may hold more agents than half its cells (its shared memory then
- * limits the SM to about four CTAs). */
+/* Threads per tile CTA: 128 for sparse tiles (nine CTAs per SM) and for
+ * 512-cell tiles, 256 when a tile of 1024 cells or more may hold more
+ * agents than half its cells (its shared memory then limits the SM to about
+ * four CTAs). */
 constexpr int NT_SPARSE = 128, NT_DENSE = 256;
 /* Resident CTAs per SM the register allocation is bounded for: 56
  * registers a thread for 128-thread CTAs (nine per SM; 48 registers, ten
@@ -670,7 +671,8 @@ void launch_one(const WorldDev &w, uint32_t grid, size_t smem,
 /* Thread count of a world's tile CTAs (see NT_SPARSE / NT_DENSE). */
 inline int step_threads(const WorldDev &w)
 {
-	return 2u * w.act_cap > (1u << w.log_tile) ? NT_DENSE : NT_SPARSE;
+	const uint32_t T = 1u << w.log_tile;
+	return 2u * w.act_cap > T && T >= 1024 ? NT_DENSE : NT_SPARSE;
 }
 
 template <bool ACT>
@@ -691,6 +693,7 @@ cudaError_t launch_step(const WorldDev &w, const LaunchCfg &lc,
 		}
 	} else {
 		switch (T / NT_SPARSE) {
+		case 4: launch_one<4, NT_SPARSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
 		case 8: launch_one<8, NT_SPARSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
 		case 16: launch_one<16, NT_SPARSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
 		case 32: launch_one<32, NT_SPARSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
@@ -736,7 +739,8 @@ cudaError_t enqueue_move_groups(const WorldDev &w, const LaunchCfg &lc,
 
 cudaError_t set_step_smem_limits(size_t bytes)
 {
-	cudaError_t e = set_step_limit<8, NT_SPARSE>(bytes);
+	cudaError_t e = set_step_limit<4, NT_SPARSE>(bytes);
+	if (e == cudaSuccess) e = set_step_limit<8, NT_SPARSE>(bytes);
 	if (e == cudaSuccess) e = set_step_limit<16, NT_SPARSE>(bytes);
 	if (e == cudaSuccess) e = set_step_limit<32, NT_SPARSE>(bytes);
 	if (e == cudaSuccess) e = set_step_limit<64, NT_SPARSE>(bytes);

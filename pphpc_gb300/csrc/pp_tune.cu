@@ -177,13 +177,14 @@ extern "C" int pp_autotune(const PPParameters *params, uint64_t seed,
 	spec.p = q;
 	spec.seed = seed;
 	spec.iters = 0xffffffffu;
-	const uint32_t tiles[4] = {1024, 2048, 4096, 8192};
+	const uint32_t tiles[5] = {512, 1024, 2048, 4096, 8192};
 	pp_tuning best{};
 	double best_cost = 1e300;
 	int last_err = PP_SUCCESS;
 	for (int fused = 1; fused >= 0; fused--) {
 		for (uint32_t t : tiles) {
 			if (t > 4 * qcells && t != 1024) continue;   /* tiles far larger than the grid */
+			if (t < 1024 && !fused) continue;            /* the sort pipeline's act needs 1024+ */
 			double c = measure(spec, cap, device, fused != 0, t, warm, timed);
 			if (c < 0) {
 				last_err = (int) c;

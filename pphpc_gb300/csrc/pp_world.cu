@@ -48,11 +48,12 @@ void choose_geometry(uint32_t total_cells, uint32_t cap, WorldConfig &cfg)
 {
 	if (cfg.tile_cells == 0) {
 		/* Dense worlds (many agents per cell) take smaller tiles so a
-		 * tile's agents fit in shared memory; the fused act is latency
-		 * bound per tile and prefers more, smaller tiles in flight (eight
-		 * 128-thread CTAs per SM) than the sort pipeline's act. */
+		 * tile's agents fit in shared memory (the fused act: 512-cell
+		 * tiles of 128 threads); the fused act is latency bound per tile
+		 * and prefers more, smaller tiles in flight (nine 128-thread CTAs
+		 * per SM) than the sort pipeline's act. */
 		double dens = total_cells ? (double) cap / total_cells : 1.0;
-		if (dens > 1.0) cfg.tile_cells = 1024;
+		if (dens > 1.0) cfg.tile_cells = cfg.fused ? 512 : 1024;
 		else cfg.tile_cells = cfg.fused ? 2048 : 4096;
 	}
 }
@@ -151,7 +152,8 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	choose_geometry((uint32_t) std::min<uint64_t>(total_cells, 0xffffffffu),
 		cfg.cap, cfg);
 	uint32_t T = cfg.tile_cells;
-	if (T != 1024 && T != 2048 && T != 4096 && T != 8192) return PP_INVALID_ARGS;
+	if (T != 1024 && T != 2048 && T != 4096 && T != 8192
+		&& !(T == 512 && cfg.fused)) return PP_INVALID_ARGS;
 	uint32_t log_tile = 0;
 	while ((1u << log_tile) < T) log_tile++;
 

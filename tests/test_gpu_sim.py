@@ -35,6 +35,18 @@ def test_tile_sizes_agree(tile, sort_pipeline):
     _check_run(params(70, 2), 5, 150, tile_cells=tile, sort_pipeline=sort_pipeline)
 
 
+@pytest.mark.parametrize("side,version,pool", [(70, 2, 0), (200, 2, 40), (150, 1, 0)])
+def test_512_cell_tiles(side, version, pool):
+    """The fused pipeline's 512-cell tiles (128-thread CTAs, crowded tiles
+    at v2 densities); the sort pipeline refuses them."""
+    p = params(side, version)
+    cap = pool * (p.init_sheep + p.init_wolves) if pool else 0
+    _check_run(p, 6, 120, tile_cells=512, max_agents=cap)
+    with pytest.raises(pp.PPError) as ei:
+        pp.Simulation(p, 6, tile_cells=512, sort_pipeline=True)
+    assert ei.value.code == pp.PP_INVALID_ARGS
+
+
 @pytest.mark.parametrize("digit_bits", [5, 6, 8])
 def test_digit_widths_agree(digit_bits):
     _check_run(params(60, 1), 4, 150, digit_bits=digit_bits, sort_pipeline=True)

@@ -13,7 +13,8 @@ pytestmark = pytest.mark.gpu
 def test_autotune_returns_a_candidate_and_caches():
     p = params(300, 2, iters=200)
     t1 = pp.autotune(p, 5)
-    assert t1["tile_cells"] in (1024, 2048, 4096, 8192)
+    assert t1["tile_cells"] in (512, 1024, 2048, 4096, 8192)
+    assert t1["tile_cells"] >= 1024 or t1["sort_pipeline"] == 0
     assert t1["ns_per_agent_step"] > 0
     t2 = pp.autotune(p, 5)
     assert t2 == t1
