@@ -94,7 +94,7 @@ class PPServeOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("mem_budget_bytes", C.c_uint64),
                 ("max_runs", C.c_uint32), ("pool_factor", C.c_uint32),
                 ("stats_chunk", C.c_uint32), ("ss_from", C.c_uint32),
-                ("agent_size", C.c_uint32)]
+                ("agent_size", C.c_uint32), ("tile_cells", C.c_uint32)]
 
 
 class PPServeEvent(C.Structure):
@@ -420,7 +420,7 @@ class Server:
     """Continuous-batching server (pp_serve_* of the C ABI)."""
 
     def __init__(self, mem_budget_bytes=8 << 30, max_runs=256, pool_factor=4,
-                 stats_chunk=64, device=0, ss_from=1000, agent_size=0):
+                 stats_chunk=64, device=0, ss_from=1000, agent_size=0, tile_cells=0):
         L = lib()
         o = PPServeOpts()
         L.pp_serve_opts_default(C.byref(o))
@@ -431,6 +431,7 @@ class Server:
         o.stats_chunk = stats_chunk
         o.ss_from = ss_from
         o.agent_size = agent_size
+        o.tile_cells = tile_cells
         self._h = C.c_void_p()
         _check(L.pp_serve_create(C.byref(o), C.byref(self._h)), "pp_serve_create")
 

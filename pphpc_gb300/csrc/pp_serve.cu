@@ -80,6 +80,8 @@ extern "C" int pp_serve_create(const pp_serve_opts *opts, pp_server **out)
 	if (opts) o = *opts;
 	else pp_serve_opts_default(&o);
 	if (o.max_runs == 0 || o.max_runs > 60000) return PP_INVALID_ARGS;
+	if (o.tile_cells != 0 && o.tile_cells != 512 && o.tile_cells != 1024
+		&& o.tile_cells != 2048) return PP_INVALID_ARGS;
 	if (o.agent_size != 0 && o.agent_size != 32 && o.agent_size != 64)
 		return PP_INVALID_ARGS;
 	pp_server *srv = new (std::nothrow) pp_server();
@@ -90,7 +92,7 @@ extern "C" int pp_serve_create(const pp_serve_opts *opts, pp_server **out)
 	 * (three key/value arrays for sorting a new run's agents, two group
 	 * buffers of three slots per agent, seven scratch words for crowded
 	 * tiles, sort look-back). Cells are bounded by the 2^31 key space. */
-	const uint32_t T = 1024;
+	const uint32_t T = o.tile_cells ? o.tile_cells : 1024;
 	const uint64_t tile_bytes = T * 2ull + 610;
 	uint64_t budget = o.mem_budget_bytes;
 	uint64_t cell_bytes = budget / 8;
@@ -112,7 +114,7 @@ extern "C" int pp_serve_create(const pp_serve_opts *opts, pp_server **out)
 	cfg.graph_iters = 0;
 	/* Dense v2 runs put up to ~2.2 agents per cell in a tile; tiles above
 	 * the shared-memory capacity take the act's crowded path. */
-	cfg.act_cap = 2048;
+	cfg.act_cap = std::min<uint32_t>(2 * T, 2048);
 	std::vector<RunSpec> none;
 	int rc = srv->world.create(none, cfg);
 	if (rc) {
@@ -143,7 +145,8 @@ extern "C" int pp_serve_submit(pp_server *srv, const pp_run_desc *run,
 	rc = agent_energy_bits(srv->opts.agent_size, p, &rq.spec.energy_bits);
 	if (rc) return rc;
 	rq.reserve = reservation(rq.spec, srv->opts.pool_factor ? srv->opts.pool_factor : 4);
-	uint64_t tiles_needed = ((uint64_t) p.grid_xy + 1023) / 1024;
+	const uint64_t T = srv->world.tile_cells();
+	uint64_t tiles_needed = ((uint64_t) p.grid_xy + T - 1) / T;
 	if (rq.reserve > srv->cap || tiles_needed > srv->max_tiles)
 		return PP_OUT_OF_RESOURCES; /* can never be admitted */
 	rq.rows.resize((size_t) p.iters + 1);

@@ -111,3 +111,24 @@ def test_serve_rejects_oversized():
         srv.submit(params(3200, 2, iters=10), 1)
     assert e.value.code == pp.PP_OUT_OF_RESOURCES
     srv.close()
+
+
+@pytest.mark.parametrize("tile", [512, 2048])
+def test_serve_tile_sizes(tile):
+    """The server's tile size option gives the same results as the oracle."""
+    srv = pp.Server(mem_budget_bytes=1 << 30, max_runs=4, stats_chunk=16,
+                    tile_cells=tile)
+    reqs = [(params(s, v, iters=60), 70 + i)
+            for i, (s, v) in enumerate([(90, 2), (41, 1), (300, 1)])]
+    ids = [srv.submit(p, seed) for p, seed in reqs]
+    for _ in range(100):
+        q, r = srv.load()
+        if q == 0 and r == 0:
+            break
+        srv.poll(16)
+    for rid, (p, seed) in zip(ids, reqs):
+        assert srv.status(rid).done == 1
+        assert first_diff(rows_array(srv.read(rid)), orc.run(p, seed)) is None
+    srv.close()
+    with pytest.raises(pp.PPError):
+        pp.Server(tile_cells=4096)
