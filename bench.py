@@ -478,15 +478,14 @@ def run_served(args, dist):
             continue
         srv.poll(16)
         now = time.perf_counter() - t0
-        for rid in list(pending):
+        for rid in srv.finished():
             ev = srv.status(rid)
-            if ev.done:
-                if ev.status != 0:
-                    raise RuntimeError("request %d failed (%d)" % (rid, ev.status))
-                rows = srv.read(rid)
-                steps += sum(r.sheep + r.wolves for r in rows[:-1])
-                lat.append(now - pending.pop(rid))
-                srv.release(rid)
+            if ev.status != 0:
+                raise RuntimeError("request %d failed (%d)" % (rid, ev.status))
+            rows = srv.read(rid)
+            steps += sum(r.sheep + r.wolves for r in rows[:-1])
+            lat.append(now - pending.pop(rid))
+            srv.release(rid)
     wall = time.perf_counter() - t0
     srv.close()
     lat.sort()

@@ -395,6 +395,12 @@ int pp_serve_status(pp_server *srv, uint64_t id, pp_serve_event *ev);
 /* Number of queued and resident runs. */
 int pp_serve_load(pp_server *srv, uint32_t *queued, uint32_t *resident);
 
+/* Ids of requests that finished (completed, failed or cancelled) since the
+ * last call, oldest first: up to `max` into ids, their number in *n_out.
+ * Lets a client poll without a status call per pending request. */
+int pp_serve_finished(pp_server *srv, uint64_t *ids, uint32_t max,
+	uint32_t *n_out);
+
 /* The focal measures of a finished request (PP_INVALID_ARGS until it has
  * finished successfully). */
 int pp_serve_focal(pp_server *srv, uint64_t id, pp_focal *out);

@@ -179,6 +179,7 @@ ABI = {
                                 _P(PPStatistics), _u32p]),
     "pp_serve_status": (C.c_int, [C.c_void_p, C.c_uint64, _P(PPServeEvent)]),
     "pp_serve_load": (C.c_int, [C.c_void_p, _u32p, _u32p]),
+    "pp_serve_finished": (C.c_int, [C.c_void_p, _P(C.c_uint64), C.c_uint32, _u32p]),
     "pp_serve_release": (C.c_int, [C.c_void_p, C.c_uint64]),
     "pp_serve_destroy": (C.c_int, [C.c_void_p]),
     "pp_autotune": (C.c_int, [_P(PPParameters), C.c_uint64, C.c_uint32, C.c_int,
@@ -453,6 +454,14 @@ class Server:
         ev = PPServeEvent()
         _check(lib().pp_serve_status(self._h, rid, C.byref(ev)), "pp_serve_status")
         return ev
+
+    def finished(self, max_ids=4096):
+        """Ids of requests finished since the last call (pp_serve_finished)."""
+        ids = (C.c_uint64 * max_ids)()
+        n = C.c_uint32()
+        _check(lib().pp_serve_finished(self._h, ids, max_ids, C.byref(n)),
+               "pp_serve_finished")
+        return list(ids)[:n.value]
 
     def load(self):
         q, r = C.c_uint32(), C.c_uint32()

@@ -26,6 +26,7 @@ extern "C" int pp_params_check(const PPParameters *p, char *errmsg, size_t errle
 namespace {
 
 struct Request {
+	uint64_t id = 0;
 	RunSpec spec;
 	int status = PP_SUCCESS;
 	uint32_t slot = 0;
@@ -52,6 +53,11 @@ struct pp_server {
 	World world;
 	pp_serve_opts opts;
 	std::deque<uint64_t> queue;
+	std::deque<uint64_t> finished;      /* done, not yet listed by pp_serve_finished */
+	/* pinned host copy of the stats ring rows one poll produced, every
+	 * slot up to the highest resident one */
+	PPStatistics *ring_host = nullptr;
+	~pp_server() { if (ring_host) cudaFreeHost(ring_host); }
 	std::map<uint64_t, Request> reqs;
 	std::vector<uint64_t> slot_req;
 	uint64_t next_id = 1;
@@ -122,6 +128,13 @@ extern "C" int pp_serve_create(const pp_serve_opts *opts, pp_server **out)
 		cudaGetLastError();
 		return rc;
 	}
+	if (cudaMallocHost(&srv->ring_host, (size_t) cfg.ring_rows * o.max_runs
+			* sizeof(PPStatistics)) != cudaSuccess) {
+		cudaGetLastError();
+		srv->ring_host = nullptr;
+		delete srv;
+		return PP_OUT_OF_RESOURCES;
+	}
 	srv->cap = (uint32_t) cap;
 	srv->max_tiles = (uint32_t) tiles;
 	srv->slot_req.assign(o.max_runs, 0);
@@ -151,6 +164,7 @@ extern "C" int pp_serve_submit(pp_server *srv, const pp_run_desc *run,
 		return PP_OUT_OF_RESOURCES; /* can never be admitted */
 	rq.rows.resize((size_t) p.iters + 1);
 	uint64_t rid = srv->next_id++;
+	rq.id = rid;
 	srv->reqs.emplace(rid, std::move(rq));
 	srv->queue.push_back(rid);
 	if (id) *id = rid;
@@ -176,6 +190,7 @@ static int finish_request(pp_server *srv, Request &rq, int status)
 	}
 	rq.done = true;
 	rq.status = status;
+	srv->finished.push_back(rq.id);
 	return rc;
 }
 
@@ -236,18 +251,23 @@ extern "C" int pp_serve_poll(pp_server *srv, uint32_t n_iters)
 		return srv->fatal = rc;
 	}
 	uint32_t g1 = g0 + steps;
-	for (uint32_t s = 0; s < srv->slot_req.size(); s++) {
+	/* rows g0 + 1 .. g1 of every slot up to the highest resident one, in
+	 * one copy (a resident run has read every row up to g0) */
+	uint32_t nslots = 0;
+	for (uint32_t s = 0; s < srv->slot_req.size(); s++)
+		if (srv->slot_req[s]) nslots = s + 1;
+	rc = w.read_ring(g0 + 1, g1, nslots, srv->ring_host);
+	if (rc) return srv->fatal = rc;
+	for (uint32_t s = 0; s < nslots; s++) {
 		uint64_t id = srv->slot_req[s];
 		if (!id) continue;
 		Request &rq = srv->reqs[id];
 		uint32_t last = rq.start_g + rq.spec.iters;
 		uint32_t lo = rq.start_g + rq.n_rows;
 		uint32_t hi = std::min(g1, last);
-		if (hi >= lo) {
-			rc = w.read_rows(s, lo, hi, rq.rows.data() + (lo - rq.start_g));
-			if (rc) return srv->fatal = rc;
-			rq.n_rows = hi - rq.start_g + 1;
-		}
+		for (uint32_t g = lo; g <= hi; g++)
+			rq.rows[g - rq.start_g] = srv->ring_host[(size_t) (g - g0 - 1) * nslots + s];
+		if (hi >= lo) rq.n_rows = hi - rq.start_g + 1;
 		if (hi == last) finish_request(srv, rq, PP_SUCCESS);
 	}
 	return PP_SUCCESS;
@@ -286,6 +306,19 @@ extern "C" int pp_serve_status(pp_server *srv, uint64_t id, pp_serve_event *ev)
 	ev->status = rq.status;
 	ev->n_rows = rq.n_rows;
 	ev->done = rq.done ? 1 : 0;
+	return PP_SUCCESS;
+}
+
+extern "C" int pp_serve_finished(pp_server *srv, uint64_t *ids, uint32_t max,
+	uint32_t *n_out)
+{
+	if (!srv || !n_out || (max && !ids)) return PP_INVALID_ARGS;
+	uint32_t n = 0;
+	while (n < max && !srv->finished.empty()) {
+		ids[n++] = srv->finished.front();
+		srv->finished.pop_front();
+	}
+	*n_out = n;
 	return PP_SUCCESS;
 }
 

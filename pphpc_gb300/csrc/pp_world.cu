@@ -545,6 +545,26 @@ int World::read_rows(uint32_t r, uint32_t g0, uint32_t g1, PPStatistics *out)
 	return PP_SUCCESS;
 }
 
+int World::read_ring(uint32_t g0, uint32_t g1, uint32_t nslots, PPStatistics *out)
+{
+	if (g1 < g0 || nslots == 0) return PP_SUCCESS;
+	PP_CK(cudaSetDevice(device_));
+	const uint32_t R = w_.ring_rows;
+	const size_t pitch = (size_t) w_.nruns_cap * sizeof(PPStatistics);
+	uint32_t g = g0;
+	while (g <= g1) {
+		uint32_t pos = g % R;
+		uint32_t cnt = std::min<uint32_t>(g1 - g + 1, R - pos);
+		PP_CK(cudaMemcpy2DAsync(out + (size_t) (g - g0) * nslots,
+			nslots * sizeof(PPStatistics), &w_.ring[(size_t) pos * w_.nruns_cap],
+			pitch, nslots * sizeof(PPStatistics), cnt, cudaMemcpyDeviceToHost, s_));
+		d2h_ += (uint64_t) cnt * nslots * sizeof(PPStatistics);
+		g += cnt;
+	}
+	PP_CK(cudaStreamSynchronize(s_));
+	return PP_SUCCESS;
+}
+
 int World::get_state(uint32_t *cell, uint32_t *en, uint32_t n_max,
 	uint32_t *n_out, uint16_t *grass, uint32_t r)
 {

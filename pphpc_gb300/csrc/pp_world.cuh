@@ -75,6 +75,10 @@ public:
 	/* Copy the stats rows of run r for world iterations [g0, g1] (ring
 	 * positions must still be valid). */
 	int read_rows(uint32_t r, uint32_t g0, uint32_t g1, PPStatistics *out);
+	/* Rows of world iterations [g0, g1] of run slots [0, nslots), row by
+	 * row (out[(g - g0) * nslots + r]), in one copy per contiguous part of
+	 * the ring. */
+	int read_ring(uint32_t g0, uint32_t g1, uint32_t nslots, PPStatistics *out);
 
 	/* Admission of a run into a free slot and tile range (serving). */
 	int admit(const RunSpec &spec, uint32_t *slot_out);

@@ -62,6 +62,7 @@ def test_serve_alone_equals_mix():
         if q == 0 and r == 0:
             break
         srv.poll(16)
+    assert sorted(srv.finished()) == sorted(ids) and srv.finished() == []
     for rid, (p, seed) in zip(ids, reqs):
         ev = srv.status(rid)
         assert ev.done == 1 and ev.status == 0
