@@ -757,8 +757,22 @@ __global__ void __launch_bounds__(ACT_THREADS) k_stats_run(WorldDev w,
 		if (v & TYPE_BIT) { acc.wolves++; acc.wen += en; }
 		else { acc.sheep++; acc.sen += en; }
 	}
-	for (uint32_t lc = blockIdx.x * blockDim.x + threadIdx.x; lc < run.ncells;
-		lc += stride) {
+	/* the run's cells start on a tile boundary (16-byte aligned): eight
+	 * countdowns per 16-byte load, then the tail */
+	const uint4 *g8 = reinterpret_cast<const uint4 *>(w.grass + run.cbase);
+	const uint32_t n8 = run.ncells / 8;
+	for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n8; q += stride) {
+		const uint4 v = g8[q];
+		const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+		for (int k = 0; k < 4; k++) {
+			const uint32_t lo = wv[k] & 0xffffu, hi = wv[k] >> 16;
+			acc.galive += (lo == 0) + (hi == 0);
+			acc.gen += lo + hi;
+		}
+	}
+	for (uint32_t lc = n8 * 8 + blockIdx.x * blockDim.x + threadIdx.x;
+		lc < run.ncells; lc += stride) {
 		uint32_t gq = w.grass[run.cbase + lc];
 		acc.galive += gq == 0;
 		acc.gen += gq;
@@ -879,8 +893,8 @@ cudaError_t enqueue_init_agents(const RunDev &run, uint32_t *k, uint32_t *v,
 cudaError_t enqueue_stats_run(const WorldDev &w, const RunDev &run,
 	uint32_t r, const uint32_t *vals, uint32_t n, uint32_t row, cudaStream_t s)
 {
-	uint32_t sb = (max(n, run.ncells) + ACT_THREADS - 1) / ACT_THREADS;
-	if (sb > 1024) sb = 1024;
+	uint32_t sb = (max(n, run.ncells / 8) + ACT_THREADS - 1) / ACT_THREADS;
+	if (sb > 2048) sb = 2048;
 	if (sb == 0) sb = 1;
 	k_stats_run<<<sb, ACT_THREADS, 0, s>>>(w, run, vals, n,
 		&w.ring[(size_t) row * w.nruns_cap + r]);
