@@ -36,11 +36,18 @@ __global__ void __launch_bounds__(256) k_radix_hist(const uint32_t *keys,
 		uint32_t i = base + threadIdx.x;
 		bool valid = i < n;
 		uint32_t k = valid ? keys[i] : 0;
+		/* one atomic per warp where the warp's digits agree (the high
+		 * digits of nearly sorted keys), else one per lane (random keys:
+		 * few collisions) */
+		const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
 		for (uint32_t p = 0; p < P; p++) {
-			uint32_t dig = valid ? ((k >> (p * d)) & mask) : 0xffffffffu;
-			uint32_t peers = __match_any_sync(0xffffffffu, dig);
-			if (valid && lane == (uint32_t) (__ffs(peers) - 1))
-				atomicAdd(&sh[(p << d) + dig], __popc(peers));
+			const uint32_t dig = (k >> (p * d)) & mask;
+			const uint32_t d0 = __shfl_sync(0xffffffffu, dig, 0);
+			if (__all_sync(0xffffffffu, !valid || dig == d0)) {
+				if (lane == 0 && vmask) atomicAdd(&sh[(p << d) + d0], __popc(vmask));
+			} else if (valid) {
+				atomicAdd(&sh[(p << d) + dig], 1u);
+			}
 		}
 	}
 	__syncthreads();
