@@ -6,6 +6,11 @@
  *            [-a AGENT_SIZE] [--iters N] [-i PROF_FILE] [-t TILE]
  *            [--digit-bits B] [--no-graph] [--dump TYPE]
  *
+ * The reference's OpenCL tuning options (-c/--compiler, --a-rng, --a-sort,
+ * --a-sort-opts, --l-*, --vw-*) are accepted with their argument and have
+ * no effect here (a note goes to stderr), so existing command lines run
+ * unchanged.
+ *
  * -p/-s/-r/-d/-m/-a keep the reference's meaning and defaults (config.txt,
  * stats.txt, seed 0, device 0, agent pool, 64-bit agents: -a sets the
  * width of the energy field, 16 bits for 64 and 11 bits for 32, with the
@@ -64,11 +69,36 @@ int main(int argc, char **argv)
 		{"no-graph", no_argument, 0, 'G'},
 		{"dump", required_argument, 0, 'U'},
 		{"help", no_argument, 0, 'h'},
+		/* the reference's OpenCL options (pp_gpu.c:310-410), without effect */
+		{"compiler", required_argument, 0, 'c'},
+		{"a-rng", required_argument, 0, 'X'},
+		{"a-sort", required_argument, 0, 'X'},
+		{"a-sort-opts", required_argument, 0, 'X'},
+		{"l-def", required_argument, 0, 'X'},
+		{"l-init-cell", required_argument, 0, 'X'},
+		{"l-init-agent", required_argument, 0, 'X'},
+		{"l-grass", required_argument, 0, 'X'},
+		{"l-reduce-grass", required_argument, 0, 'X'},
+		{"l-reduce-agent", required_argument, 0, 'X'},
+		{"l-move-agent", required_argument, 0, 'X'},
+		{"l-sort-agent", required_argument, 0, 'X'},
+		{"l-find-index", required_argument, 0, 'X'},
+		{"l-action-agent", required_argument, 0, 'X'},
+		{"vw-grass", required_argument, 0, 'X'},
+		{"vw-reduce-grass", required_argument, 0, 'X'},
+		{"vw-reduce-agent", required_argument, 0, 'X'},
 		{0, 0, 0, 0}
 	};
-	int c;
-	while ((c = getopt_long(argc, argv, "p:s:r:d:m:a:i:t:h", longopts, NULL)) != -1) {
+	int c, li = 0;
+	while ((c = getopt_long(argc, argv, "p:s:r:d:m:a:i:t:c:h", longopts, &li)) != -1) {
 		switch (c) {
+		case 'c':
+			fprintf(stderr, "Note: -c/--compiler has no effect here (OpenCL option)\n");
+			break;
+		case 'X':
+			fprintf(stderr, "Note: --%s has no effect here (OpenCL option)\n",
+				longopts[li].name);
+			break;
 		case 'p': params_file = optarg; break;
 		case 's': stats_file = optarg; break;
 		case 'r': seed = strtoll(optarg, NULL, 0); break;

@@ -87,3 +87,13 @@ def test_cli_agent_size_argument(tmp_path):
     r = _cli("--agent-size", "32", "-p", str(f), "-s", str(tmp_path / "s.txt"))
     assert r.returncode == pp.PP_INVALID_ARGS & 0xff
     assert "-a 64" in r.stderr
+
+
+def test_cli_accepts_the_references_opencl_options():
+    """OpenCL tuning options of the reference parse (with a note) and have no
+    effect: the run goes on to the agent-size check."""
+    r = _cli("--a-sort", "s-bitonic", "--a-sort-opts", "lws=64", "--a-rng", "lcg",
+             "--l-def", "64", "--vw-grass", "4", "-c", "-cl-fast-relaxed-math",
+             "-a", "48", "-p", os.path.join(GOLDEN, "config100v1.txt"))
+    assert r.returncode == pp.PP_INVALID_ARGS & 0xff
+    assert "--a-sort has no effect" in r.stderr and "-c/--compiler" in r.stderr
