@@ -284,6 +284,16 @@ int pp_radix_sort_host(uint32_t n, const uint32_t *keys_in,
 	const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out,
 	uint32_t key_bits, uint32_t digit_bits);
 
+/* Failure-detection self-test of the bounded device-side waits: n_chunks
+ * (<= 4096) chunks of one launch run the finish kernel's decoupled
+ * look-back, each publishing chunk + 1; prefix_out (n_chunks words, may be
+ * NULL) receives each chunk's exclusive prefix. With stall_chunk >= 0 that
+ * chunk never publishes: the wait behind it gives up after a bounded number
+ * of polls and the call returns PP_ERR_TIMEOUT, the device staying usable;
+ * with -1 it returns PP_SUCCESS and prefix_out[k] = k (k + 1) / 2. */
+int pp_lookback_selftest(uint32_t n_chunks, int32_t stall_chunk,
+	uint32_t *prefix_out);
+
 /* Largest n accepted by pp_radix_sort_noalloc. */
 #define PP_NOALLOC_SORT_MAX_N (1u << 22)
 

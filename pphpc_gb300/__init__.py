@@ -161,6 +161,7 @@ ABI = {
     "pp_sim_dump": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_char_p]),
     "pp_sim_restore": (C.c_int, [C.c_char_p, _P(PPOpts), _P(C.c_void_p)]),
     "pp_philox_fill": (C.c_int, [C.c_uint32] * 7 + [_u32p]),
+    "pp_lookback_selftest": (C.c_int, [C.c_uint32, C.c_int32, _u32p]),
     "pp_move_host": (C.c_int, [_P(PPParameters), C.c_uint64, C.c_uint32, C.c_uint32,
                                _u32p, _u32p, _u32p, _u32p]),
     "pp_radix_sort_host": (C.c_int, [C.c_uint32, _u32p, _u32p, _u32p, _u32p,
@@ -377,6 +378,16 @@ def run(params, seed=0, iters=None, **kw):
     iters = params.iters if iters is None else iters
     with Simulation(params, seed, **kw) as sim:
         return [sim.stats0()] + sim.step(iters)
+
+
+def lookback_selftest(n_chunks, stall_chunk=-1):
+    """Bounded-wait self-test (pp_lookback_selftest): the chunks' exclusive
+    prefixes; raises PPError(PP_ERR_TIMEOUT) when stall_chunk >= 0."""
+    import numpy as np
+    out = np.zeros(n_chunks, np.uint32)
+    _check(lib().pp_lookback_selftest(n_chunks, stall_chunk, out.ctypes.data_as(_u32p)),
+           "pp_lookback_selftest")
+    return out
 
 
 def release_cached_memory(device=-1):

@@ -186,9 +186,9 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *a,
 /* Warp-wide decoupled look-back (lanes read 32 predecessors at once).
  * Called by all lanes of one warp; returns the exclusive prefix of `tile`
  * and publishes its inclusive prefix. Bounded: a predecessor that does not
- * publish within SPIN_LIMIT polls raises ERRF_TIMEOUT. */
+ * publish within `limit` polls raises ERRF_TIMEOUT. */
 __device__ uint32_t warp_lookback(uint64_t *lb, uint32_t tile, uint32_t agg,
-	uint32_t epoch, uint32_t *err)
+	uint32_t epoch, uint32_t *err, uint32_t limit = SPIN_LIMIT)
 {
 	const uint32_t lane = threadIdx.x & 31;
 	if (tile == 0) {
@@ -215,7 +215,7 @@ __device__ uint32_t warp_lookback(uint64_t *lb, uint32_t tile, uint32_t agg,
 				val = 0;
 			}
 			if (__all_sync(0xffffffffu, flag != 0)) break;
-			if (++spins > SPIN_LIMIT) { timed_out = true; break; }
+			if (++spins > limit) { timed_out = true; break; }
 			if (spins > 32) __nanosleep(64);
 		}
 		if (timed_out) {
@@ -781,6 +781,22 @@ __global__ void __launch_bounds__(ACT_THREADS) k_stats_run(WorldDev w,
 	if (threadIdx.x < 6) stats_atomic_add(dst, threadIdx.x, s_part[threadIdx.x]);
 }
 
+/* Self-test of the bounded look-back the finish kernel uses: one warp per
+ * chunk (chunks taken by ticket, so a chunk's predecessors are running or
+ * done) publishes chunk + 1 and looks back; chunk `stall` never publishes,
+ * so the wait of the chunk after it runs out after `limit` polls and raises
+ * ERRF_TIMEOUT instead of hanging. */
+__global__ void k_lookback_selftest(uint64_t *lb, uint32_t *ticket, uint32_t *err,
+	uint32_t *prefix, uint32_t stall, uint32_t limit)
+{
+	uint32_t chunk = 0;
+	if (threadIdx.x == 0) chunk = atomicAdd(ticket, 1u);
+	chunk = __shfl_sync(0xffffffffu, chunk, 0);
+	if (chunk == stall) return;
+	const uint32_t excl = warp_lookback(lb, chunk, chunk + 1, 1u, err, limit);
+	if (threadIdx.x == 0) prefix[chunk] = excl;
+}
+
 __global__ void k_philox_fill(uint32_t c0, uint32_t c1, uint32_t c2,
 	uint32_t c3, uint32_t k0, uint32_t k1, uint32_t n, uint32_t *out)
 {
@@ -898,6 +914,13 @@ cudaError_t enqueue_stats_run(const WorldDev &w, const RunDev &run,
 	if (sb == 0) sb = 1;
 	k_stats_run<<<sb, ACT_THREADS, 0, s>>>(w, run, vals, n,
 		&w.ring[(size_t) row * w.nruns_cap + r]);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_lookback_selftest(uint64_t *lb, uint32_t *ticket, uint32_t *err,
+	uint32_t *prefix, uint32_t n, uint32_t stall, uint32_t limit, cudaStream_t s)
+{
+	k_lookback_selftest<<<n, 32, 0, s>>>(lb, ticket, err, prefix, stall, limit);
 	return cudaGetLastError();
 }
 

@@ -87,6 +87,11 @@ cudaError_t enqueue_fused_bases(const WorldDev &w, const LaunchCfg &lc,
 
 cudaError_t set_step_smem_limits(size_t bytes);
 
+/* Bounded look-back self-test over n chunks (chunk `stall` never
+ * publishes; `limit` polls per wait). */
+cudaError_t launch_lookback_selftest(uint64_t *lb, uint32_t *ticket, uint32_t *err,
+	uint32_t *prefix, uint32_t n, uint32_t stall, uint32_t limit, cudaStream_t s);
+
 /* Focal measures of run r restarted from its stats row `row` (its
  * iteration t0). */
 cudaError_t enqueue_focal_init(const WorldDev &w, uint32_t r, uint32_t row,

@@ -1313,6 +1313,30 @@ extern "C" int pp_move_host(const PPParameters *params, uint64_t seed,
 	return PP_SUCCESS;
 }
 
+extern "C" int pp_lookback_selftest(uint32_t n_chunks, int32_t stall_chunk,
+	uint32_t *prefix_out)
+{
+	if (n_chunks == 0 || n_chunks > 4096) return PP_INVALID_ARGS;
+	DevBuf lb, misc, pre;
+	PP_CK(lb.alloc((size_t) n_chunks * 8));
+	PP_CK(misc.alloc(8));
+	PP_CK(pre.alloc((size_t) n_chunks * 4));
+	PP_CK(cudaMemset(lb.p, 0, (size_t) n_chunks * 8));
+	PP_CK(cudaMemset(misc.p, 0, 8));
+	PP_CK(cudaMemset(pre.p, 0, (size_t) n_chunks * 4));
+	uint32_t *ticket = misc.as<uint32_t>(), *err = ticket + 1;
+	/* about 2^14 polls (tens of milliseconds) before a wait gives up */
+	PP_CK(launch_lookback_selftest(lb.as<uint64_t>(), ticket, err,
+		pre.as<uint32_t>(), n_chunks,
+		stall_chunk < 0 ? 0xffffffffu : (uint32_t) stall_chunk, 1u << 14, 0));
+	PP_CK(cudaDeviceSynchronize());
+	uint32_t e = 0;
+	PP_CK(cudaMemcpy(&e, err, 4, cudaMemcpyDeviceToHost));
+	if (prefix_out)
+		PP_CK(cudaMemcpy(prefix_out, pre.p, (size_t) n_chunks * 4, cudaMemcpyDeviceToHost));
+	return (e & ERRF_TIMEOUT) ? PP_ERR_TIMEOUT : PP_SUCCESS;
+}
+
 extern "C" int pp_radix_sort_host(uint32_t n, const uint32_t *keys_in,
 	const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out,
 	uint32_t key_bits, uint32_t digit_bits)
