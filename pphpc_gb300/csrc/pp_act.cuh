@@ -1,7 +1,7 @@
 /*
  * pp_act.cuh -- device logic shared by the sort pipeline (pp_kernels.cu)
  * and the fused act+move pipeline (pp_fused.cu): the random walk and its
- * inverse, the actions of one cell's agents, stats accumulation.
+ * inverse, the actions of an agent in its cell, stats accumulation.
  */
 #pragma once
 

@@ -154,9 +154,10 @@ __device__ __forceinline__ uint32_t step_excl_scan(uint32_t v, uint32_t *total)
  *         survivors and newborns into the group buffer of parity t + 1.
  *   !ACT: the move of iteration 1 of a freshly initialised run's agents,
  *         read cell-sorted from kS/vS at the tile offsets.
- * Phases (ACT): gather; counting sort by cell with each multi-agent cell's
- * list put in canonical order; B draws; C actions (as the sort pipeline's
- * act); E0 output offsets and stats; E1 move draws and per-class counts;
+ * Phases (ACT): gather; counting sort by cell, each agent of a multi-agent
+ * cell placed by its rank in canonical order; B draws; C actions, one
+ * thread per agent (as the sort pipeline's act); E0 output offsets and
+ * stats; E1 move draws and per-class counts;
  * one warp allocates the tile's groups and posts them to the destination
  * tiles' inboxes; E2 records into the groups; per-tile stats. */
 template <int CPT, int NT, bool ACT>
