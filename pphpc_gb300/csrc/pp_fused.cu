@@ -479,155 +479,155 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 				while (f > 0 && LK[f - 1] == lk) f--;
 			rank = o - (ACT ? LP[f] : f);
 			en = nb ? LD[j] : (LV[j] & ENERGY_MASK);
-	};
+		};
 
-	/* ---- E1: move draws of the outputs, per-class counts; with room in
-	 * the cell counters' words (2 act_cap <= T), each output's key bits and
-	 * class are kept for E2, else only its direction ---- */
-	bool bad = false;
-	const bool cache = in_smem && 2u * w.act_cap <= (uint32_t) (CPT * NT);
-	uint32_t *DEST = scnt;
-	for (uint32_t o = tid; o < total; o += NT) {
-		uint32_t j, nb, en, rank;
-		output(o, j, nb, en, rank);
-		const uint32_t lc = LK[j] & 0xffffu;
-		uint32_t code, cls, klo = lc;
-		if (!live_move) {
-			code = DIR_PARKED;
-			cls = CLS_GRAVE;
-		} else if (((en - 1) & run.emask) == 0) {
-			code = DIR_DEAD;
-			cls = CLS_GRAVE;
-		} else {
-			const u4 r = rng(seed_lo, seed_hi, lt0 + lc, tmove, STREAM_MOVE, rank);
-			code = draw(r.x, 5);
-			const uint32_t dg = run.cbase + move_dir(run, lt0 + lc, code);
-			const uint32_t dt = dg >> w.log_tile;
-			klo = dg & lcmask;
-			cls = dt == tile ? CLS_OWN : class_insert(s_tbl, dt);
-		}
-		if (cls == CLS_NONE || rank > REC_RANK_MAX) {
-			bad = true;
-			cls = NCLS;                      /* counted nowhere */
-		}
-		if (cache) DEST[o] = klo | (code << REC_DIR_SHIFT) | (cls << 16);
-		else DIR[o] = (uint8_t) code;
-		warp_agg_add(s_ccnt, cls);
-	}
-	if (bad) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
-	__syncthreads();
-
-	/* ---- the tile's groups: one per class, laid out in class order
-	 * from its slots ---- */
-	uint32_t my_c = 0, my_start = 0;
-	if (tid < 32) {
-		my_c = s_ccnt[lane];
-		uint32_t x = my_c;
-#pragma unroll
-		for (int o = 1; o < 32; o <<= 1) {
-			const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-			if (lane >= (uint32_t) o) x += y;
-		}
-		const bool fail = (uint64_t) gb + total > 3ull * w.cap;
-		if (lane == 0) {
-			s_fail = fail;
-			if (fail) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
-		}
-		my_start = gb + x - my_c;
-		s_cpos[lane] = my_start;
-	}
-	__syncthreads();
-
-	if (!s_fail) {
-		/* the groups are posted to their destination tiles' inboxes by
-		 * warp 0 while the records are written */
-		uint32_t slot = IBX;
-		size_t ib = 0;
-		if (tid < 32 && my_c) {
-			const uint32_t dt = lane < CLS_FOREIGN ? s_tbl[lane] : tile;
-			ib = (size_t) pout * w.n_tiles + dt;
-			slot = atomicAdd(&w.inbox_n[ib], 1u);
-		}
-		/* ---- E2: records into the groups ---- */
-		uint32_t *kGo = pout ? w.kG1 : w.kG0;
-		uint32_t *vGo = pout ? w.vG1 : w.vG0;
+		/* ---- E1: move draws of the outputs, per-class counts; with room in
+		 * the cell counters' words (2 act_cap <= T), each output's key bits and
+		 * class are kept for E2, else only its direction ---- */
+		bool bad = false;
+		const bool cache = in_smem && 2u * w.act_cap <= (uint32_t) (CPT * NT);
+		uint32_t *DEST = scnt;
 		for (uint32_t o = tid; o < total; o += NT) {
 			uint32_t j, nb, en, rank;
 			output(o, j, nb, en, rank);
 			const uint32_t lc = LK[j] & 0xffffu;
-			const uint32_t tb = LV[j] & TYPE_BIT;
-			uint32_t key, val, cls;
-			if (cache) {
-				const uint32_t d = DEST[o];
-				const uint32_t code = (d >> REC_DIR_SHIFT) & 7u;
-				cls = d >> 16;
-				key = (d & 0xffffu) | (rank << REC_RANK_SHIFT);
-				val = code >= DIR_PARKED ? (tb | en) : (tb | ((en - 1) & run.emask));
+			uint32_t code, cls, klo = lc;
+			if (!live_move) {
+				code = DIR_PARKED;
+				cls = CLS_GRAVE;
+			} else if (((en - 1) & run.emask) == 0) {
+				code = DIR_DEAD;
+				cls = CLS_GRAVE;
+			} else {
+				const u4 r = rng(seed_lo, seed_hi, lt0 + lc, tmove, STREAM_MOVE, rank);
+				code = draw(r.x, 5);
+				const uint32_t dg = run.cbase + move_dir(run, lt0 + lc, code);
+				const uint32_t dt = dg >> w.log_tile;
+				klo = dg & lcmask;
+				cls = dt == tile ? CLS_OWN : class_insert(s_tbl, dt);
+			}
+			if (cls == CLS_NONE || rank > REC_RANK_MAX) {
+				bad = true;
+				cls = NCLS;                      /* counted nowhere */
+			}
+			if (cache) DEST[o] = klo | (code << REC_DIR_SHIFT) | (cls << 16);
+			else DIR[o] = (uint8_t) code;
+			warp_agg_add(s_ccnt, cls);
+		}
+		if (bad) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
+		__syncthreads();
+
+		/* ---- the tile's groups: one per class, laid out in class order
+		 * from its slots ---- */
+		uint32_t my_c = 0, my_start = 0;
+		if (tid < 32) {
+			my_c = s_ccnt[lane];
+			uint32_t x = my_c;
+#pragma unroll
+			for (int o = 1; o < 32; o <<= 1) {
+				const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+				if (lane >= (uint32_t) o) x += y;
+			}
+			const bool fail = (uint64_t) gb + total > 3ull * w.cap;
+			if (lane == 0) {
+				s_fail = fail;
+				if (fail) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
+			}
+			my_start = gb + x - my_c;
+			s_cpos[lane] = my_start;
+		}
+		__syncthreads();
+
+		if (!s_fail) {
+			/* the groups are posted to their destination tiles' inboxes by
+			 * warp 0 while the records are written */
+			uint32_t slot = IBX;
+			size_t ib = 0;
+			if (tid < 32 && my_c) {
+				const uint32_t dt = lane < CLS_FOREIGN ? s_tbl[lane] : tile;
+				ib = (size_t) pout * w.n_tiles + dt;
+				slot = atomicAdd(&w.inbox_n[ib], 1u);
+			}
+			/* ---- E2: records into the groups ---- */
+			uint32_t *kGo = pout ? w.kG1 : w.kG0;
+			uint32_t *vGo = pout ? w.vG1 : w.vG0;
+			for (uint32_t o = tid; o < total; o += NT) {
+				uint32_t j, nb, en, rank;
+				output(o, j, nb, en, rank);
+				const uint32_t lc = LK[j] & 0xffffu;
+				const uint32_t tb = LV[j] & TYPE_BIT;
+				uint32_t key, val, cls;
+				if (cache) {
+					const uint32_t d = DEST[o];
+					const uint32_t code = (d >> REC_DIR_SHIFT) & 7u;
+					cls = d >> 16;
+					key = (d & 0xffffu) | (rank << REC_RANK_SHIFT);
+					val = code >= DIR_PARKED ? (tb | en) : (tb | ((en - 1) & run.emask));
+					const uint32_t pos = warp_agg_add(s_cpos, cls);
+					if (cls != NCLS) {
+						kGo[pos] = key;
+						vGo[pos] = val;
+					}
+					continue;
+				}
+				const uint32_t code = DIR[o];
+				if (code >= DIR_PARKED) {
+					cls = CLS_GRAVE;
+					key = lc | (code << REC_DIR_SHIFT) | (rank << REC_RANK_SHIFT);
+					val = tb | en;
+				} else {
+					const uint32_t dg = run.cbase + move_dir(run, lt0 + lc, code);
+					const uint32_t dt = dg >> w.log_tile;
+					cls = dt == tile ? CLS_OWN : class_find(s_tbl, dt);
+					key = (dg & lcmask) | (code << REC_DIR_SHIFT) | (rank << REC_RANK_SHIFT);
+					val = tb | ((en - 1) & run.emask);
+				}
+				if (cls == CLS_NONE || rank > REC_RANK_MAX) cls = NCLS;
 				const uint32_t pos = warp_agg_add(s_cpos, cls);
 				if (cls != NCLS) {
 					kGo[pos] = key;
 					vGo[pos] = val;
 				}
-				continue;
 			}
-			const uint32_t code = DIR[o];
-			if (code >= DIR_PARKED) {
-				cls = CLS_GRAVE;
-				key = lc | (code << REC_DIR_SHIFT) | (rank << REC_RANK_SHIFT);
-				val = tb | en;
-			} else {
-				const uint32_t dg = run.cbase + move_dir(run, lt0 + lc, code);
-				const uint32_t dt = dg >> w.log_tile;
-				cls = dt == tile ? CLS_OWN : class_find(s_tbl, dt);
-				key = (dg & lcmask) | (code << REC_DIR_SHIFT) | (rank << REC_RANK_SHIFT);
-				val = tb | ((en - 1) & run.emask);
-			}
-			if (cls == CLS_NONE || rank > REC_RANK_MAX) cls = NCLS;
-			const uint32_t pos = warp_agg_add(s_cpos, cls);
-			if (cls != NCLS) {
-				kGo[pos] = key;
-				vGo[pos] = val;
+			if (tid < 32 && my_c) {
+				if (slot < IBX)
+					w.inbox[ib * IBX + slot] = make_uint2(my_start,
+						my_c | (lane == CLS_GRAVE ? GROUP_GRAVE : 0u));
+				else
+					atomicOr(&w.ctr->err, ERRF_OVERFLOW);
 			}
 		}
-		if (tid < 32 && my_c) {
-			if (slot < IBX)
-				w.inbox[ib * IBX + slot] = make_uint2(my_start,
-					my_c | (lane == CLS_GRAVE ? GROUP_GRAVE : 0u));
-			else
-				atomicOr(&w.ctr->err, ERRF_OVERFLOW);
-		}
-	}
 
-	/* ---- per-tile partial stats (ACT); the tile's eating events go to the
-	 * run's regrowth histogram slot of iteration t + restart ---- */
-	if (ACT) {
-		__shared__ uint64_t red[5][NT / 32];
-		const uint32_t wid = tid >> 5;
-		const uint32_t sw = warp_sum(sheep | (wolves << 16));
-		const uint32_t ew = warp_sum(eats);
-		const uint64_t se = warp_sum(sen), we = warp_sum(wen);
-		if (lane == 0) {
-			red[0][wid] = sw & 0xffffu;
-			red[1][wid] = sw >> 16;
-			red[2][wid] = ew;
-			red[3][wid] = se;
-			red[4][wid] = we;
-		}
-		__syncthreads();
-		if (tid < 5) {
-			uint64_t sum = 0;
-			for (uint32_t q = 0; q < NT / 32; q++) sum += red[tid][q];
-			if (tid == 2) {
-				if (sum)
-					atomicAdd(&w.fring[run.fbase + (t + run.restart) % (run.restart + 1)],
-						(uint32_t) sum);
-				w.part[(size_t) tile * 8 + 2] = 0;
-				w.part[(size_t) tile * 8 + 5] = 0;
-			} else {
-				w.part[(size_t) tile * 8 + tid] = sum;
+		/* ---- per-tile partial stats (ACT); the tile's eating events go to the
+		 * run's regrowth histogram slot of iteration t + restart ---- */
+		if (ACT) {
+			__shared__ uint64_t red[5][NT / 32];
+			const uint32_t wid = tid >> 5;
+			const uint32_t sw = warp_sum(sheep | (wolves << 16));
+			const uint32_t ew = warp_sum(eats);
+			const uint64_t se = warp_sum(sen), we = warp_sum(wen);
+			if (lane == 0) {
+				red[0][wid] = sw & 0xffffu;
+				red[1][wid] = sw >> 16;
+				red[2][wid] = ew;
+				red[3][wid] = se;
+				red[4][wid] = we;
+			}
+			__syncthreads();
+			if (tid < 5) {
+				uint64_t sum = 0;
+				for (uint32_t q = 0; q < NT / 32; q++) sum += red[tid][q];
+				if (tid == 2) {
+					if (sum)
+						atomicAdd(&w.fring[run.fbase + (t + run.restart) % (run.restart + 1)],
+							(uint32_t) sum);
+					w.part[(size_t) tile * 8 + 2] = 0;
+					w.part[(size_t) tile * 8 + 5] = 0;
+				} else {
+					w.part[(size_t) tile * 8 + tid] = sum;
+				}
 			}
 		}
-	}
 	};
 	if (in_smem) {
 		phases(std::true_type{}, sk, sv, sperm, sp, sd);
