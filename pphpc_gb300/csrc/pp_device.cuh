@@ -73,7 +73,9 @@ struct u4 { uint32_t x, y, z, w; };
 __host__ __device__ __forceinline__ u4 philox4x32_10(u4 c, uint32_t k0,
 	uint32_t k1)
 {
+#ifdef __CUDA_ARCH__
 #pragma unroll
+#endif
 	for (int r = 0; r < 10; r++) {
 #ifdef __CUDA_ARCH__
 		uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
