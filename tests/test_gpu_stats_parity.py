@@ -31,7 +31,7 @@ def _port_fms(p, seeds):
     return np.array([focal_measures(r, p.grid_x * p.grid_y, SS_FROM) for r in runs])
 
 
-@pytest.mark.parametrize("side,version,pool_factor", [(100, 1, 8), (400, 2, 40)])
+@pytest.mark.parametrize("side,version,pool_factor", [(100, 1, 8), (200, 2, 40), (400, 2, 40)])
 def test_gpu_vs_cpu_algorithm(side, version, pool_factor):
     p = params(side, version, iters=4000)
     a = _gpu_fms(p, range(REPS), pool_factor)
