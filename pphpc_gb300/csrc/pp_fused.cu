@@ -221,9 +221,10 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 	if (tid < CLS_FOREIGN) s_tbl[tid] = TBL_EMPTY;
 	if (tid <= NCLS) s_ccnt[tid] = 0;
 	if (tid == NCLS) s_cpos[NCLS] = 0;
-	/* per-cell counters, transposed: cell c at SLOT(c) = (c % CPT) * NT +
-	 * c / CPT, so no two threads of a warp share a bank */
-#define SLOT(c) ((((c) % CPT) * NT) + (c) / CPT)
+	/* per-cell counters, transposed in groups of four: thread k's cells
+	 * k CPT + 4 a .. + 3 are the 16 bytes at word 4 (a NT + k), so a warp
+	 * reads its threads' counters with conflict-free 16-byte loads */
+#define SLOT(c) (((((c) % CPT) >> 2) * NT + (c) / CPT) * 4 + ((c) & 3))
 	if (ACT) {
 		uint4 *z = reinterpret_cast<uint4 *>(scnt);
 #pragma unroll
@@ -332,18 +333,25 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 			__syncthreads();
 			if (tid == 0) w.inbox_n[(size_t) pin * w.n_tiles + tile] = 0;
 			{
+				uint4 *s4 = reinterpret_cast<uint4 *>(scnt);
 				uint32_t loc = 0;
 #pragma unroll
-				for (int q = 0; q < CPT; q++) {
-					loc += scnt[q * NT + tid];
+				for (int a = 0; a < CPT / 4; a++) {
+					const uint4 v = s4[a * NT + tid];
+					loc += v.x + v.y + v.z + v.w;
 				}
 				uint32_t tot;
 				uint32_t run_start = step_excl_scan<NT>(loc, &tot);
 #pragma unroll
-				for (int q = 0; q < CPT; q++) {
-					const uint32_t c = scnt[q * NT + tid];
-					scnt[q * NT + tid] = run_start;
-					run_start += c;
+				for (int a = 0; a < CPT / 4; a++) {
+					const uint4 v = s4[a * NT + tid];
+					uint4 o;
+					o.x = run_start;
+					o.y = o.x + v.x;
+					o.z = o.y + v.y;
+					o.w = o.z + v.z;
+					run_start = o.w + v.w;
+					s4[a * NT + tid] = o;
 				}
 			}
 			__syncthreads();
