@@ -64,7 +64,8 @@ def test_without_graph():
 
 
 @pytest.mark.parametrize("gx,gy,s,w", [(1, 1, 5, 3), (1, 50, 20, 10), (50, 1, 20, 10),
-                                       (7, 13, 40, 20), (300, 2, 30, 30)])
+                                       (7, 13, 40, 20), (300, 2, 30, 30),
+                                       (65535, 2, 3000, 1500), (2, 65535, 3000, 1500)])
 @PIPES
 def test_degenerate_grids(gx, gy, s, w, sort_pipeline):
     _check_run(params(0, 1, gx=gx, gy=gy, sheep=s, wolves=w), 3, 120,
