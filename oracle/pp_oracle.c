@@ -33,7 +33,9 @@
  *               gain is modulo 2^energy_bits); every agent that
  *               acts then reproduces if energy > threshold and
  *               draw(Philox({c, t, ACT, k}).w1, 100) < prob: the child
- *               gets energy/2 and the parent keeps the rest. Newborns
+ *               gets energy/2 (0 for a parent of energy 1 under a
+ *               threshold of 0: the child exists all the same) and the
+ *               parent keeps the rest. Newborns
  *               neither act nor are eaten in their birth iteration.
  *               Output (the cell's next list): its agents in rank order,
  *               each surviving agent followed by its newborn (if any).
@@ -260,7 +262,8 @@ int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
 	uint32_t *cell_out, uint32_t *en_out, uint32_t cap)
 {
 	uint32_t *fin = malloc(sizeof(uint32_t) * (n ? n : 1));   /* final energy */
-	uint32_t *kid = malloc(sizeof(uint32_t) * (n ? n : 1));   /* child energy, 0 = none */
+	uint32_t *kid = malloc(sizeof(uint32_t) * (n ? n : 1));   /* child energy */
+	uint8_t *haskid = malloc(n ? n : 1);   /* a child (its energy may be 0) */
 	uint8_t *eaten = malloc(n ? n : 1);
 	ord_t *ord = malloc(sizeof(ord_t) * (n ? n : 1));
 	uint32_t *dice = malloc(sizeof(uint32_t) * (n ? n : 1));
@@ -281,6 +284,7 @@ int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
 			dice[s] = ppo_draw(r[1], 100);
 			fin[s] = energy_of(en[s]);
 			kid[s] = 0;
+			haskid[s] = 0;
 			eaten[s] = 0;
 			if (type_of(en[s])) W++; else S++;
 		}
@@ -310,8 +314,11 @@ int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
 				thr = p->sheep_thr; prob = p->sheep_prob;
 			}
 			if (acts && fin[s] > thr && dice[s] < prob) {
+				/* the child exists even at energy 0 (a parent of energy 1
+				 * under a threshold of 0), as in pp_gpu.cl:948-960 */
 				kid[s] = fin[s] / 2;
 				fin[s] -= kid[s];
+				haskid[s] = 1;
 			}
 		}
 		grass[c] = (uint16_t) g;
@@ -323,13 +330,13 @@ int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
 			if (out < cap) { cell_out[out] = cell[s]; en_out[out] = tb | fin[s]; }
 			out++;
 		}
-		if (kid[s]) {
+		if (haskid[s]) {
 			if (out < cap) { cell_out[out] = cell[s]; en_out[out] = tb | kid[s]; }
 			out++;
 		}
 	}
 	ret = out > cap ? -8 : (int64_t) out;
-	free(fin); free(kid); free(eaten); free(ord); free(dice);
+	free(fin); free(kid); free(haskid); free(eaten); free(ord); free(dice);
 	return ret;
 }
 

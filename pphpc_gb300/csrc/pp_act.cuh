@@ -84,8 +84,9 @@ struct ActParams {
  * cell's live grass (g0 == 0) iff it acts and no sheep before it acts.
  * LV[i] keeps its type bit throughout, so the agents of a cell read each
  * other's types while they write their results. On return LV[j] holds type
- * | final energy, or type | EATEN_BIT, and *kid the newborn's energy (0 =
- * none); the result is true iff agent j eats the grass. */
+ * | final energy, or type | EATEN_BIT, and *kid KID_BIT | the newborn's
+ * energy (which is 0 for a parent of energy 1 under a threshold of 0), or 0
+ * for no newborn; the result is true iff agent j eats the grass. */
 __device__ __forceinline__ bool act_agent(uint32_t j, uint32_t p, uint32_t e,
 	uint32_t *LV, const uint32_t *LP, const ActParams &ap, uint32_t g0,
 	uint32_t dice, uint32_t *kid)
@@ -130,9 +131,10 @@ __device__ __forceinline__ bool act_agent(uint32_t j, uint32_t p, uint32_t e,
 	if (grass) en = (en + ap.sheep_gain) & ap.emask;
 	const uint32_t thr = tb ? ap.wolves_thr : ap.sheep_thr;
 	const uint32_t prob = tb ? ap.wolves_prob : ap.sheep_prob;
-	const uint32_t k = (acts && en > thr && dice < prob) ? en >> 1 : 0;
+	const bool rep = acts && en > thr && dice < prob;
+	const uint32_t k = rep ? en >> 1 : 0;
 	LV[j] = tb | (eaten ? EATEN_BIT : en - k);
-	*kid = k;
+	*kid = rep ? KID_BIT | k : 0u;
 	return grass;
 }
 

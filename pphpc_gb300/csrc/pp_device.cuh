@@ -30,9 +30,12 @@ namespace pp {
 
 constexpr uint32_t TYPE_BIT = 0x80000000u;
 constexpr uint32_t ENERGY_MASK = 0x7fffffffu;
-/* Marks an agent eaten in the act phase's per-agent words (above every
- * energy field width). */
+/* Marks an agent eaten in the act phase's per-agent words, and a newborn
+ * in its parent's newborn word (whose energy may be 0): above every energy
+ * field width. */
 constexpr uint32_t EATEN_BIT = 0x40000000u;
+constexpr uint32_t KID_BIT = 0x40000000u;
+constexpr uint32_t KID_ENERGY = KID_BIT - 1;
 
 /* Energy field mask for a width of bits (11, 16 or 30). */
 __host__ __device__ __forceinline__ uint32_t energy_mask_of(uint32_t bits)

@@ -429,9 +429,10 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 					cnt++;
 					if (tb) { wolves++; wen += en; } else { sheep++; sen += en; }
 				}
-				if (kd) {
+				if (kd & KID_BIT) {
 					cnt++;
-					if (tb) { wolves++; wen += kd; } else { sheep++; sen += kd; }
+					const uint32_t ke = kd & KID_ENERGY;
+					if (tb) { wolves++; wen += ke; } else { sheep++; sen += ke; }
 				}
 			}
 		}
@@ -451,7 +452,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 					if (in_smem) OUTJ16[o] = (uint16_t) j; else OUTJ32[o] = j;
 					o++;
 				}
-				if (LD[j]) {
+				if (LD[j] & KID_BIT) {
 					if (in_smem) OUTJ16[o] = (uint16_t) (j | 0x8000u);
 					else OUTJ32[o] = j | 0x80000000u;
 					o++;
@@ -486,7 +487,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 			if (!ACT)
 				while (f > 0 && LK[f - 1] == lk) f--;
 			rank = o - (ACT ? LP[f] : f);
-			en = nb ? LD[j] : (LV[j] & ENERGY_MASK);
+			en = nb ? (LD[j] & KID_ENERGY) : (LV[j] & ENERGY_MASK);
 		};
 
 		/* ---- E1: move draws of the outputs, per-class counts; with room in

@@ -388,7 +388,7 @@ __global__ void __launch_bounds__(ACT_THREADS, 5) k_act(WorldDev w,
 		const uint32_t ja = min(tid * ch, m), jb = min(ja + ch, m);
 		uint32_t cnt = 0;
 		for (uint32_t j = ja; j < jb; j++)
-			cnt += ((LV[j] & EATEN_BIT) == 0) + (LD[j] != 0);
+			cnt += ((LV[j] & EATEN_BIT) == 0) + ((LD[j] & KID_BIT) != 0);
 		uint32_t total;
 		const uint32_t excl = block_excl_scan(cnt, &total);
 		const uint32_t rs = 2 * a0;
@@ -409,12 +409,13 @@ __global__ void __launch_bounds__(ACT_THREADS, 5) k_act(WorldDev w,
 				if (tb) { wolves++; wen += en; }
 				else { sheep++; sen += en; }
 			}
-			if (kd) {
+			if (kd & KID_BIT) {
+				const uint32_t ke = kd & KID_ENERGY;
 				w.kR[o] = k;
-				w.vR[o] = tb | kd;
+				w.vR[o] = tb | ke;
 				o++;
-				if (tb) { wolves++; wen += kd; }
-				else { sheep++; sen += kd; }
+				if (tb) { wolves++; wen += ke; }
+				else { sheep++; sen += ke; }
 			}
 		}
 		/* per-tile partial stats; the tile's eating events go to the run's

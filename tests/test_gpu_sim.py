@@ -156,3 +156,21 @@ def test_cached_device_buffers_reused_and_released():
     again = rows_array(pp.run(p, 3))
     assert first_diff(first, want) is None and first_diff(again, want) is None
     assert pp.release_cached_memory() >= cached
+
+
+@PIPES
+def test_threshold_zero_newborns_of_energy_zero(sort_pipeline):
+    """Under a reproduction threshold of 0 a parent of energy 1 has a child
+    of energy 0, which exists (pp_gpu.cl:948-960) and, by the modular
+    decrement, leaves its first move with the field's maximum energy."""
+    p = params(60, 1, iters=40)
+    p.sheep_reproduce_threshold = 0
+    p.wolves_reproduce_threshold = 0
+    cap = 40 * (p.init_sheep + p.init_wolves)
+    _check_run(p, 4, 40, sort_pipeline=sort_pipeline, max_agents=cap)
+    st = orc.State(p, 4, capacity=cap)
+    for _ in range(40):
+        st.step()
+    _, en = st.agents()
+    st.close()
+    assert ((en & 0x3fffffff) == 0x3fffffff).any()

@@ -83,12 +83,13 @@ def _seq_cell(order, types, energy, dice, grass, p):
     """Sequential list semantics of pp_cpu.cl:640-848 for one cell whose
     agents act in `order`: wolves eat the first sheep still in the list
     (acted or not); a sheep removed before its turn does not act; the
-    acting sheep eats live grass; acting agents reproduce. Returns final
-    energies (0 = eaten), newborn energies and the grass."""
+    acting sheep eats live grass; acting agents reproduce (a child exists
+    even at energy 0). Returns final energies (0 = eaten), newborn energies
+    (None = no newborn) and the grass."""
     alive = {j: True for j in order}
     lst = list(order)
     en = dict(energy)
-    kid = {j: 0 for j in order}
+    kid = {j: None for j in order}
     for j in order:
         if not alive[j]:
             continue
@@ -147,7 +148,7 @@ def test_act_closed_form_matches_sequential_lists(case):
         tb = int(types[s]) << 31
         if fin[s]:
             want.append(tb | fin[s])
-        if kid[s]:
+        if kid[s] is not None:
             want.append(tb | kid[s])
     assert list(eo) == want
     assert list(co) == [7] * len(want)
