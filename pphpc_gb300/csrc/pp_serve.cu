@@ -233,6 +233,7 @@ static int admit_queued(pp_server *srv)
 
 extern "C" int pp_serve_poll(pp_server *srv, uint32_t n_iters)
 {
+	pp::NvtxRange nvtx_range("pp_serve_poll");
 	if (!srv) return PP_INVALID_ARGS;
 	if (srv->fatal) return srv->fatal;
 	World &w = srv->world;

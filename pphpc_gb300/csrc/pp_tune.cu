@@ -134,6 +134,7 @@ double measure(const RunSpec &spec, uint32_t cap, int device, bool fused,
 extern "C" int pp_autotune(const PPParameters *params, uint64_t seed,
 	uint32_t max_agents, int device, pp_tuning *out)
 {
+	pp::NvtxRange nvtx_range("pp_autotune");
 	if (!params || !out) return PP_INVALID_ARGS;
 	PPParameters p = *params;
 	p.grid_xy = p.grid_x * p.grid_y;

@@ -134,6 +134,7 @@ int agent_energy_bits(uint32_t agent_size, const PPParameters &p, uint32_t *bits
 
 int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 {
+	pp::NvtxRange nvtx_range("world create");
 	WorldConfig cfg = cfg_in;
 	device_ = cfg.device;
 	PP_CK(cudaSetDevice(device_));
@@ -785,6 +786,7 @@ bool World::fits(const RunSpec &spec) const
 
 int World::admit(const RunSpec &spec, uint32_t *slot_out)
 {
+	pp::NvtxRange nvtx_range("admit");
 	PP_CK(cudaSetDevice(device_));
 	uint32_t need = ceil_div((uint64_t) spec.p.grid_x * spec.p.grid_y,
 		1u << w_.log_tile);
@@ -949,6 +951,7 @@ extern "C" void pp_opts_default(pp_opts *o)
 static int sim_create(const PPParameters *params, uint64_t seed,
 	const pp_opts *opts, const RunSpec *spec0, pp_sim **out)
 {
+	pp::NvtxRange nvtx_range("pp_sim_create");
 	if (!params || !out) return PP_INVALID_ARGS;
 	*out = nullptr;
 	PPParameters p = *params;
@@ -1023,6 +1026,7 @@ static const char SNAP_MAGIC_V1[8] = {'P', 'P', 'S', 'N', 'A', 'P', '0', '1'};
 
 extern "C" int pp_sim_snapshot_save(pp_sim *sim, const char *path)
 {
+	pp::NvtxRange nvtx_range("pp_sim_snapshot_save");
 	if (!sim || !path) return PP_INVALID_ARGS;
 	World &w = sim->world;
 	uint32_t n = 0;
@@ -1136,6 +1140,7 @@ extern "C" int pp_sim_stats0(pp_sim *sim, PPStatistics *out)
 
 extern "C" int pp_sim_step(pp_sim *sim, uint32_t n_iters, PPStatistics *out)
 {
+	pp::NvtxRange nvtx_range("pp_sim_step");
 	if (!sim) return PP_INVALID_ARGS;
 	World &w = sim->world;
 	const uint32_t chunk_max = w.ring_rows() - 1;
@@ -1443,6 +1448,7 @@ extern "C" int pp_batch_autotune(const pp_run_desc *runs, int n_runs,
 extern "C" int pp_batch_run(const pp_run_desc *runs, int n_runs,
 	const pp_batch_opts *opts, pp_stats_cb cb, void *user)
 {
+	pp::NvtxRange nvtx_range("pp_batch_run");
 	if (!runs || n_runs <= 0) return PP_INVALID_ARGS;
 	pp_batch_opts o;
 	if (opts) o = *opts;

@@ -10,9 +10,20 @@
 #include <vector>
 #include <cstring>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "pp_kernels.cuh"
 
 namespace pp {
+
+/* A named NVTX range over a host-side phase (create, step, admission, poll,
+ * tuning), for timeline tools; without one attached it costs nothing. */
+struct NvtxRange {
+	explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+	~NvtxRange() { nvtxRangePop(); }
+	NvtxRange(const NvtxRange &) = delete;
+	NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 struct RunSpec {
 	PPParameters p;
