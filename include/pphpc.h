@@ -66,16 +66,20 @@ typedef struct pp_parameters {
 } PPParameters;
 
 /* Per-iteration statistics (opencl/pp/pp_common.in.h:109-124). Row k is the
- * state after k iterations. The energy and countdown sums are 64-bit here
- * because the reference's 32-bit sums overflow on a 12800x12800 grid. */
+ * state after k iterations. The fields are the reference's, in the
+ * reference's order (errors last); the energy and countdown sums are 64-bit
+ * here because the reference's 32-bit sums overflow on a 12800x12800 grid.
+ * Layout (48 bytes, natural alignment): sheep 0, wolves 4, grass 8, 4 bytes
+ * of padding, sheep_en 16, wolves_en 24, grass_en 32, errors 40, 4 bytes of
+ * padding. */
 typedef struct pp_statistics {
 	uint32_t sheep;
 	uint32_t wolves;
 	uint32_t grass;    /* cells with countdown == 0                    */
-	uint32_t errors;   /* pool-overflow events (0 in a successful run) */
 	uint64_t sheep_en;
 	uint64_t wolves_en;
 	uint64_t grass_en; /* sum of grass countdowns                      */
+	uint32_t errors;   /* pool-overflow events (0 in a successful run) */
 } PPStatistics;
 
 /* ------------------------------------------------------------------ */

@@ -25,7 +25,10 @@
  *   4. act    -- per cell c, agents in increasing (priority, k) order,
  *               priority = Philox({c, t, ACT, k}).w0 for new rank k.
  *               This is the sequential semantics of pp_cpu.cl:596-866
- *               with the shuffle replaced by the priority order:
+ *               with the shuffle replaced by the priority order, run
+ *               literally as the reference's scan of the cell's list
+ *               (ppo_act; the CUDA path evaluates the same rules in
+ *               closed form):
  *               a wolf eats the first not-yet-eaten sheep of the cell
  *               (eaten sheep may have acted already); a sheep that is not
  *               yet eaten at its turn eats the grass if countdown == 0
@@ -257,6 +260,66 @@ static int ord_cmp(const void *a, const void *b)
 	return x->slot < y->slot ? -1 : (x->slot > y->slot);
 }
 
+void ppo_act_cell(const ppo_params *p, uint32_t m, const uint32_t *en,
+	const uint32_t *prio, const uint32_t *dice, uint32_t *grass,
+	uint32_t *fin, uint32_t *kid, uint8_t *haskid, uint8_t *eaten)
+{
+	const uint32_t emask = ppo_energy_mask(p);
+	ord_t stack_ord[64];
+	ord_t *ord = m <= 64 ? stack_ord : malloc(sizeof(ord_t) * m);
+	for (uint32_t j = 0; j < m; j++) {
+		ord[j].prio = prio[j];
+		ord[j].slot = j;
+		fin[j] = energy_of(en[j]);
+		kid[j] = 0;
+		haskid[j] = 0;
+		eaten[j] = 0;
+	}
+	/* the reference shuffles the list (pp_cpu.cl:641-686); here the list
+	 * order is (priority, rank) */
+	qsort(ord, m, sizeof(ord_t), ord_cmp);
+	/* The literal sequential scan of pp_cpu.cl:690-848 over the cell's
+	 * list in that order: eaten[] plays the part of the reference's removal
+	 * from the list (rem_ag_from_cell), so an eaten agent is skipped at its
+	 * turn and by later wolves. */
+	uint32_t g = *grass;
+	for (uint32_t j = 0; j < m; j++) {
+		uint32_t s = ord[j].slot;
+		uint32_t thr, prob;
+		if (eaten[s]) continue;        /* removed before its turn */
+		if (type_of(en[s])) {
+			/* a wolf walks the list from its head for the first sheep
+			 * still in it (acted or not), removes it and gains
+			 * (pp_cpu.cl:719-768) */
+			for (uint32_t q = 0; q < m; q++) {
+				uint32_t s2 = ord[q].slot;
+				if (eaten[s2] || type_of(en[s2])) continue;
+				eaten[s2] = 1;
+				fin[s] = (fin[s] + p->wolves_gain) & emask;
+				break;
+			}
+			thr = p->wolves_thr; prob = p->wolves_prob;
+		} else {
+			/* a sheep eats live grass (pp_cpu.cl:700-717) */
+			if (g == 0) {
+				g = p->grass_restart;
+				fin[s] = (fin[s] + p->sheep_gain) & emask;
+			}
+			thr = p->sheep_thr; prob = p->sheep_prob;
+		}
+		/* every acting agent may reproduce (pp_cpu.cl:771-837) */
+		if (fin[s] > thr && dice[s] < prob) {
+			/* the child exists even at energy 0 (a parent of energy 1
+			 * under a threshold of 0), as in pp_gpu.cl:948-960 */
+			kid[s] = fin[s] / 2;
+			fin[s] -= kid[s];
+			haskid[s] = 1;
+		}
+	}
+	*grass = g;
+	if (ord != stack_ord) free(ord);
+}
+
 int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
 	uint32_t n, const uint32_t *cell, const uint32_t *en, uint16_t *grass,
 	uint32_t *cell_out, uint32_t *en_out, uint32_t cap)
@@ -265,62 +328,25 @@ int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
 	uint32_t *kid = malloc(sizeof(uint32_t) * (n ? n : 1));   /* child energy */
 	uint8_t *haskid = malloc(n ? n : 1);   /* a child (its energy may be 0) */
 	uint8_t *eaten = malloc(n ? n : 1);
-	ord_t *ord = malloc(sizeof(ord_t) * (n ? n : 1));
+	uint32_t *prio = malloc(sizeof(uint32_t) * (n ? n : 1));
 	uint32_t *dice = malloc(sizeof(uint32_t) * (n ? n : 1));
 	uint64_t out = 0;
 	int64_t ret;
-	const uint32_t emask = ppo_energy_mask(p);
 
 	uint32_t lo = 0;
 	while (lo < n) {
 		uint32_t c = cell[lo], hi = lo;
 		while (hi < n && cell[hi] == c) hi++;
-		uint32_t m = hi - lo, S = 0, W = 0;
+		uint32_t m = hi - lo;
 		for (uint32_t j = 0; j < m; j++) {
-			uint32_t s = lo + j, r[4];
+			uint32_t r[4];
 			draw4(seed, c, iter, PPO_STREAM_ACT, j, r);
-			ord[j].prio = r[0];
-			ord[j].slot = s;
-			dice[s] = ppo_draw(r[1], 100);
-			fin[s] = energy_of(en[s]);
-			kid[s] = 0;
-			haskid[s] = 0;
-			eaten[s] = 0;
-			if (type_of(en[s])) W++; else S++;
+			prio[lo + j] = r[0];
+			dice[lo + j] = ppo_draw(r[1], 100);
 		}
-		qsort(ord, m, sizeof(ord_t), ord_cmp);
-		uint32_t sb = 0, wb = 0, g = grass[c];
-		for (uint32_t j = 0; j < m; j++) {
-			uint32_t s = ord[j].slot;
-			int acts;
-			uint32_t thr, prob;
-			if (type_of(en[s])) {
-				/* Wolf k eats the k-th sheep in order, if there is one
-				 * (pp_cpu.cl:721-763). */
-				if (wb < S) fin[s] = (fin[s] + p->wolves_gain) & emask;
-				wb++;
-				acts = 1;
-				thr = p->wolves_thr; prob = p->wolves_prob;
-			} else {
-				/* Sheep j is eaten by wolf j (if j < W); it acts iff that
-				 * wolf has not come yet: wolves before <= sheep before. */
-				acts = wb <= sb;
-				eaten[s] = sb < W;
-				sb++;
-				if (acts && g == 0) {
-					g = p->grass_restart;
-					fin[s] = (fin[s] + p->sheep_gain) & emask;
-				}
-				thr = p->sheep_thr; prob = p->sheep_prob;
-			}
-			if (acts && fin[s] > thr && dice[s] < prob) {
-				/* the child exists even at energy 0 (a parent of energy 1
-				 * under a threshold of 0), as in pp_gpu.cl:948-960 */
-				kid[s] = fin[s] / 2;
-				fin[s] -= kid[s];
-				haskid[s] = 1;
-			}
-		}
+		uint32_t g = grass[c];
+		ppo_act_cell(p, m, en + lo, prio + lo, dice + lo, &g, fin + lo,
+			kid + lo, haskid + lo, eaten + lo);
 		grass[c] = (uint16_t) g;
 		lo = hi;
 	}
@@ -336,7 +362,7 @@ int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
 		}
 	}
 	ret = out > cap ? -8 : (int64_t) out;
-	free(fin); free(kid); free(haskid); free(eaten); free(ord); free(dice);
+	free(fin); free(kid); free(haskid); free(eaten); free(prio); free(dice);
 	return ret;
 }
 

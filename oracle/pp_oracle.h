@@ -107,6 +107,16 @@ int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
 	uint32_t n, const uint32_t *cell, const uint32_t *en, uint16_t *grass,
 	uint32_t *cell_out, uint32_t *en_out, uint32_t cap);
 
+/* Actions of one cell's m agents, given by rank j (0..m-1): type | energy
+ * en[j], priority prio[j], reproduction draw dice[j] in [0, 100); *grass is
+ * the cell's countdown (updated). The agents act in increasing (priority,
+ * rank) order, run as the reference's sequential scan of the cell's list.
+ * Out per rank: fin (final energy), kid/haskid (newborn energy, presence),
+ * eaten. */
+void ppo_act_cell(const ppo_params *p, uint32_t m, const uint32_t *en,
+	const uint32_t *prio, const uint32_t *dice, uint32_t *grass,
+	uint32_t *fin, uint32_t *kid, uint8_t *haskid, uint8_t *eaten);
+
 #ifdef __cplusplus
 }
 #endif

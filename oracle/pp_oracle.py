@@ -70,6 +70,9 @@ def lib():
         L.ppo_act.argtypes = [C.POINTER(OParams), C.c_uint64, C.c_uint32, C.c_uint32,
                               _u32p, _u32p, C.POINTER(C.c_uint16), _u32p, _u32p,
                               C.c_uint32]
+        _u8p = C.POINTER(C.c_uint8)
+        L.ppo_act_cell.argtypes = [C.POINTER(OParams), C.c_uint32, _u32p, _u32p, _u32p,
+                                   _u32p, _u32p, _u32p, _u8p, _u8p]
         _lib = L
     return _lib
 

@@ -61,10 +61,11 @@ class PPParameters(C.Structure):
 
 
 class PPStatistics(C.Structure):
+    # the reference's field order (pp_common.in.h:109-124), sums widened
     _fields_ = [("sheep", C.c_uint32), ("wolves", C.c_uint32),
-                ("grass", C.c_uint32), ("errors", C.c_uint32),
-                ("sheep_en", C.c_uint64), ("wolves_en", C.c_uint64),
-                ("grass_en", C.c_uint64)]
+                ("grass", C.c_uint32), ("sheep_en", C.c_uint64),
+                ("wolves_en", C.c_uint64), ("grass_en", C.c_uint64),
+                ("errors", C.c_uint32)]
 
     def as_tuple(self):
         return (self.sheep, self.wolves, self.grass, self.sheep_en,

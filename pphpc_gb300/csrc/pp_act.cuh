@@ -87,7 +87,7 @@ struct ActParams {
  * | final energy, or type | EATEN_BIT, and *kid KID_BIT | the newborn's
  * energy (which is 0 for a parent of energy 1 under a threshold of 0), or 0
  * for no newborn; the result is true iff agent j eats the grass. */
-__device__ __forceinline__ bool act_agent(uint32_t j, uint32_t p, uint32_t e,
+__host__ __device__ __forceinline__ bool act_agent(uint32_t j, uint32_t p, uint32_t e,
 	uint32_t *LV, const uint32_t *LP, const ActParams &ap, uint32_t g0,
 	uint32_t dice, uint32_t *kid)
 {

@@ -64,3 +64,44 @@ def test_gpu_entry_fails_loudly_without_device():
         pp.lib().pp_sim_destroy(h)
     else:
         assert rc == pp.PP_ERR_CUDA
+
+
+STATS_LAYOUT = [("sheep", 0), ("wolves", 4), ("grass", 8), ("sheep_en", 16),
+                ("wolves_en", 24), ("grass_en", 32), ("errors", 40)]
+
+
+def _c_layout(tmp_path, struct, fields):
+    """sizeof/offsetof of `struct` as the C compiler lays it out from
+    include/pphpc.h."""
+    src = tmp_path / "layout.c"
+    body = "".join('printf("%%zu\\n", offsetof(%s, %s));\n' % (struct, f)
+                   for f in fields)
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "pphpc.h"\n'
+                   'int main(void) {\nprintf("%%zu\\n", sizeof(%s));\n%s'
+                   'return 0;\n}\n' % (struct, body))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], stdout=subprocess.PIPE, text=True,
+                         check=True).stdout.split()
+    return int(out[0]), [int(x) for x in out[1:]]
+
+
+def test_statistics_layout_matches_reference_order(tmp_path):
+    # the reference's field order (pp_common.in.h:109-124: sheep, wolves,
+    # grass, sheep_en, wolves_en, grass_en, errors) with 64-bit sums, in C
+    # and in the Python mirror
+    size, offs = _c_layout(tmp_path, "PPStatistics", [f for f, _ in STATS_LAYOUT])
+    assert size == 48
+    assert offs == [o for _, o in STATS_LAYOUT]
+    assert ctypes.sizeof(pp.PPStatistics) == 48
+    assert [f for f, _ in pp.PPStatistics._fields_] == [f for f, _ in STATS_LAYOUT]
+    for f, o in STATS_LAYOUT:
+        assert getattr(pp.PPStatistics, f).offset == o, f
+
+
+def test_parameters_layout_matches_reference(tmp_path):
+    # pp_common.in.h:129-157: thirteen unsigned ints in this order
+    size, offs = _c_layout(tmp_path, "PPParameters", pp.PARAM_FIELDS)
+    assert size == 4 * 13 == ctypes.sizeof(pp.PPParameters)
+    assert offs == [4 * i for i in range(13)]

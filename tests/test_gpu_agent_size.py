@@ -137,7 +137,7 @@ def test_cli_agent_size_32(tmp_path):
         assert len(lines) == p.iters + 1
         for i in range(0, p.iters + 1, 7):
             w = rows[i]
-            s = pp.PPStatistics(int(w[0]), int(w[1]), int(w[2]), 0, int(w[3]),
+            s = pp.PPStatistics(int(w[0]), int(w[1]), int(w[2]), int(w[3]),
                                 int(w[4]), int(w[5]))
             assert lines[i] == pp.format_row(s, p), (args, i)
     assert first_diff(want, orc.run(p, 3, energy_bits=16)) is not None

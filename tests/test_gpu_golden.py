@@ -51,7 +51,7 @@ def test_cli_stats_file(tmp_path):
     assert len(lines) == 4001
     for i in range(0, 4001, 50):
         r_ = want[i]
-        s = pp.PPStatistics(int(r_[0]), int(r_[1]), int(r_[2]), 0, int(r_[3]),
+        s = pp.PPStatistics(int(r_[0]), int(r_[1]), int(r_[2]), int(r_[3]),
                             int(r_[4]), int(r_[5]))
         assert lines[i] == pp.format_row(s, p), i
 

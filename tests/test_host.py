@@ -90,7 +90,7 @@ def test_stats_format_matches_reference_printf():
     p = pp.load_params(os.path.join(GOLDEN, "config100v1.txt"))
     rows = np.load(os.path.join(GOLDEN, "stats_100v1_s0.npz"))["rows"]
     for r in rows[::97]:
-        s = pp.PPStatistics(int(r[0]), int(r[1]), int(r[2]), 0, int(r[3]), int(r[4]), int(r[5]))
+        s = pp.PPStatistics(int(r[0]), int(r[1]), int(r[2]), int(r[3]), int(r[4]), int(r[5]))
         assert pp.format_row(s, p) == _ref_row([int(x) for x in r], 10000)
 
 
@@ -103,7 +103,7 @@ def test_stats_zero_counts():
 def test_stats_save(tmp_path):
     p = pp.load_params(os.path.join(GOLDEN, "config100v1.txt"))
     rows = np.load(os.path.join(GOLDEN, "stats_100v1_s0.npz"))["rows"][:11]
-    st = [pp.PPStatistics(int(r[0]), int(r[1]), int(r[2]), 0, int(r[3]), int(r[4]), int(r[5]))
+    st = [pp.PPStatistics(int(r[0]), int(r[1]), int(r[2]), int(r[3]), int(r[4]), int(r[5]))
           for r in rows]
     out = tmp_path / "stats.txt"
     pp.stats_save(str(out), st, p)
