@@ -12,8 +12,22 @@ running the oracle on the GPU host:
   stats_small.npz      short runs of small grids and edge cases (oracle);
   philox.npz           Philox4x32-10 words for a few counter/key ranges.
 
+Large fixtures (each one oracle run, minutes to an hour of one CPU core;
+made with `python tests/golden/make_golden.py large [name ...]`):
+
+  stats_12800v1_s2_r300.npz  rows 0..300 of 12800x12800 v1, seed 2, pool 5x
+      the initial agents (through the population peak near iteration 147),
+      and the SHA-256 of the canonical state after iteration 300 (agents'
+      cells and type|energy words, then the grass countdowns, as the
+      oracle lists them);
+  stats_mix_<side>v<v>_s<seed>.npz  all 4001 rows of one run of each class
+      of the 64-run batched mix: 200x200 v1 seed 100, 800x800 v2 seed 132,
+      1600x1600 v1 seed 148, 3200x3200 v2 seed 156 (the mix's first run of
+      each class).
+
 Run from the repository root: python tests/golden/make_golden.py
 """
+import hashlib
 import os
 import sys
 
@@ -63,6 +77,39 @@ SMALL = [  # name, params, seed, iters
 ]
 
 
+LARGE = {  # name: (params, seed, iterations, agent pool or 0 for the oracle's default)
+    "12800v1_s2_r300": (cfg(12800, 1), 2, 300, 5 * (6553600 + 3276800)),
+    "mix_200v1_s100": (cfg(200, 1), 100, 4000, 0),
+    "mix_800v2_s132": (cfg(800, 2), 132, 4000, 0),
+    "mix_1600v1_s148": (cfg(1600, 1), 148, 4000, 0),
+    "mix_3200v2_s156": (cfg(3200, 2), 156, 4000, 0),
+}
+
+
+def state_digest(cell, en, grass):
+    """SHA-256 of a canonical state: cells, type|energy words, grass."""
+    h = hashlib.sha256()
+    for a in (cell, en, grass):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def make_large(name):
+    d, seed, iters, pool = LARGE[name]
+    st = orc.State(d, seed, capacity=pool)
+    rows = [st.stats()]
+    for _ in range(iters):
+        rows.append(st.step())
+    cell, en = st.agents()
+    digest = state_digest(cell, en, st.grass())
+    st.close()
+    np.savez_compressed(os.path.join(HERE, "stats_%s.npz" % name),
+                        rows=np.array(rows, np.uint64),
+                        params=np.array([d[f] for f in FIELDS], np.uint32),
+                        seed=np.array([seed], np.uint64), pool=np.array([pool], np.uint64),
+                        state_sha256=np.array(digest))
+
+
 def write_config(path, d):
     with open(path, "w") as f:
         for k, fld in zip(KEYS, FIELDS):
@@ -93,4 +140,8 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "large":
+        for n in sys.argv[2:] or sorted(LARGE):
+            make_large(n)
+    else:
+        main()
