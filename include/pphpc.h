@@ -230,8 +230,8 @@ void *pp_sim_stream(pp_sim *sim);
  * the iteration number, parameters and seed -- to the file `path`. A
  * simulation restored from it continues with exactly the stats and state
  * of the uninterrupted one (every draw is keyed by cell, iteration and
- * rank, none by memory layout). No counterpart in the reference (SURVEY
- * §8(f): state snapshot / resume). */
+ * rank, none by memory layout). No counterpart in the reference (state
+ * snapshot / resume is new here). */
 int pp_sim_snapshot_save(pp_sim *sim, const char *path);
 
 /* Create a simulation from a snapshot file written by pp_sim_snapshot_save.
@@ -282,8 +282,9 @@ int pp_move_host(const PPParameters *params, uint64_t seed, uint32_t iter,
 	uint32_t n, const uint32_t *cell_in, const uint32_t *en_in,
 	uint32_t *cell_out, uint32_t *en_out);
 
-/* Stable LSD radix sort of (key, value) pairs by the low `key_bits` bits
- * (replaces the cl_ops sort call, pp_gpu.c:826-828). digit_bits 0 = auto. */
+/* Stable LSD radix sort of (key, value) pairs whose keys are below
+ * 2^key_bits (replaces the cl_ops sort call, pp_gpu.c:826-828); key_bits
+ * 1..32, digit_bits 5..8 or 0 = auto. */
 int pp_radix_sort_host(uint32_t n, const uint32_t *keys_in,
 	const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out,
 	uint32_t key_bits, uint32_t digit_bits);
@@ -305,7 +306,8 @@ int pp_lookback_selftest(uint32_t n_chunks, int32_t stall_chunk,
  * allocate device memory, such as an application whose device memory is
  * owned by its own pooling allocator, or a loop with a latency budget in
  * which cudaMalloc/cudaFree could synchronise the device. Same stable LSD
- * radix sort as pp_radix_sort_host, but on caller-owned device buffers
+ * radix sort as pp_radix_sort_host (keys below 2^key_bits), but on
+ * caller-owned device buffers
  * (`keys`, `vals` in; `keys_out`, `vals_out` out; the input buffers are
  * overwritten as ping-pong space) and with its scratch in a fixed array
  * inside the library (about 2 MB per GPU, held until the process exits).

@@ -9,7 +9,8 @@ import pphpc_gb300 as pp
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
-REF_CONFIGS = "/root/reference/configs"
+# the reference's configs directory, where the reference tree is present
+REF_CONFIGS = os.path.join(os.environ.get("PPHPC_REFERENCE", "/root/reference"), "configs")
 
 
 def test_load_golden_configs():
