@@ -21,37 +21,43 @@ ours:       W untimed iterations, then K iterations timed with CUDA events
             12 C + (16 + 16 P + 16) N bytes (C cells, N agents at the
             iteration's start, P = 4 sort passes at this grid size; the
             8 bytes per birth are left out), attributed to the fused
-            act+move kernel, which does the whole iteration but the stats.
-            `lower_bound` puts the algorithm-free 12 C + 32 N bytes per
-            iteration over the timed iterations.
-            `batched` runs the 64-run mix (32 x 200^2 v1, 16 x 800^2 v2,
-            8 x 1600^2 v1, 8 x 3200^2 v2, seeds 100..163, --batch-iters
-            iterations each) once through pp_batch_run (one world, every
-            launch shared) and once run by run through pp_sim_* (one run per
-            launch sequence), both end to end with host stats buffers, and
-            checks that every run's stats agree bit for bit.
-reference:  the CPU restatement of the reference's CPU algorithm
-            (oracle/pp_cpu_port.c: row-banded pp_cpu semantics, OpenMP over
-            all host cores; the reference itself cannot be built here) on
-            the same workload, each step one iteration.
+            act+move kernel, which does the whole iteration but the stats;
+            `dram_frac` beside it is the kernel's measured DRAM traffic
+            (ncu, profiles/ncu_traffic.json) over the same launch time.
+            Further legs (each skippable):
+            `full_run`  the whole 4000-iteration run of the workload, end to
+                        end and device-timed;
+            `batched`   the 64-run mix (32 x 200^2 v1, 16 x 800^2 v2,
+                        8 x 1600^2 v1, 8 x 3200^2 v2, seeds 100..163,
+                        --batch-iters iterations each) through pp_batch_run
+                        (one world, every launch shared) and run by run
+                        through pp_sim_*, both end to end, bit-exactness of
+                        every run, per-shape plain times and the bound they
+                        put on the batching speed-up;
+            `configs`   the reference's two small plain configs (100^2 v1
+                        seed 0, 400^2 v2 seed 1, 4000 iterations), whole
+                        runs on the GPU and by the reference's CPU kernels;
+            `served`    the 1000-request Poisson stream (below);
+            `cpu_baseline` the reference's CPU kernels on a bounded sample
+                        of the workload.
+reference:  the reference's own CPU algorithm: opencl/pp/pp_cpu.cl compiled
+            unmodified for the host (oracle/ref/build_ref.py; only its RNG,
+            from the absent cl_ops library, is a stand-in), driven by the
+            reference host's work sizes and launch loop with all host
+            threads, on the same workload and window: W untimed iterations,
+            then K iterations timed one by one (host clock).
 With N > 1 (torchrun), every rank runs an independent replica (the runs
 do not exchange data); the timed region is bracketed by barriers and the
-slowest rank's time is used.
+slowest rank's time is used. The reference arm runs on rank 0 only.
 
-  python bench.py --workload configs
+  python bench.py --workload configs | served
 
-prints one line for the reference's two small plain configs (100^2 v1 seed
-0, 400^2 v2 seed 1, 4000 iterations), each run whole on the GPU and by the
-CPU restatement on all host threads.
-
-  python bench.py --workload served
-
-prints one line for the served workload instead: a Poisson stream (20
-requests/s) of 1000 runs, side uniform in {100, ..., 3200}, parameter set
-v1 or v2 (p = 0.5), iterations uniform in [500, 4000], sequential seeds,
-admitted into one continuously batched world under a 150 GB budget; p50 /
-p99 completion latency (arrival to last stats row on the host) and
-aggregate agent-steps/s.
+prints only the `configs` or `served` leg as its own line. The served
+workload: a Poisson stream (20 requests/s) of 1000 runs, side uniform in
+{100, ..., 3200}, parameter set v1 or v2 (p = 0.5), iterations uniform in
+[500, 4000], sequential seeds, admitted into one continuously batched world
+under a 150 GB budget; p50 / p99 completion latency (arrival to last stats
+row on the host) and aggregate agent-steps/s.
 """
 import argparse
 import json
@@ -221,6 +227,9 @@ def ncu_traffic():
         return {}
 
 
+REF_MAX_AGENTS = 1 << 27   # the reference's -m for the 12800^2 workload (1 GiB of slots)
+
+
 def workload(pp, args):
     """The plain workload: 12800 x 12800 v1 by default; --side scales the
     grid (agents by area) for smaller cases of the same kernels."""
@@ -228,6 +237,81 @@ def workload(pp, args):
         return pp.make_params(**WORKLOAD), WORKLOAD_NAME
     p = scaled_params(pp, args.side, 1, WORKLOAD["iters"])
     return p, "pphpc-%dx%d-v1" % (args.side, args.side)
+
+
+def workload_dict(args):
+    """The plain workload as a parameter dict (no library needed)."""
+    wl, wname = dict(WORKLOAD), WORKLOAD_NAME
+    if args.side != 12800:
+        a = args.side * args.side
+        wl.update(grid_x=args.side, grid_y=args.side, init_sheep=a * 4 // 100,
+                  init_wolves=a * 2 // 100)
+        wname = "pphpc-%dx%d-v1" % (args.side, args.side)
+    return wl, wname
+
+
+def config_of(args, world):
+    """The `config` object, identical in both arms."""
+    wl, wname = workload_dict(args)
+    return {"workload": wname, "grid": "%dx%d" % (wl["grid_x"], wl["grid_y"]),
+            "params": "v1", "init_sheep": wl["init_sheep"],
+            "init_wolves": wl["init_wolves"], "seed": SEED,
+            "timed_iterations": "%d..%d" % (args.warmup + 1, args.warmup + args.steps),
+            "l2": "inputs larger than L2 (working set ~2 GB on the GPU)",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
+def ref_max_agents(wl):
+    """Agent slots for the reference's CPU kernels: its default (2^24) for
+    the small configs, 2^27 for larger grids (its random slot allocation
+    needs several times the live agents)."""
+    n0 = wl["init_sheep"] + wl["init_wolves"]
+    return REF_MAX_AGENTS if 8 * n0 > (1 << 24) else 0
+
+
+def cpu_sample(wl, steps, warmup):
+    """The reference's CPU kernels (all host threads) on `steps` iterations
+    after `warmup`; falls back to the single-threaded oracle where the
+    reference's kernels are unavailable."""
+    from oracle import pp_ref
+    if pp_ref.available():
+        r = pp_ref.timed_steps(wl, SEED, steps, warmup, max_agents=ref_max_agents(wl))
+        sample = ("iterations %d..%d of the %dx%d v1 workload (seed %d), each timed; "
+                  "opencl/pp/pp_cpu.cl compiled unmodified, the reference host's "
+                  "work sizes and launch loop, %d host threads, %d agent slots"
+                  % (warmup + 1, warmup + steps, wl["grid_x"], wl["grid_y"], SEED,
+                     r["cores"], ref_max_agents(wl) or 1 << 24))
+        return dict(r, kind="reference", sample=sample)
+    from oracle import pp_oracle as orc
+    st = orc.State(wl, SEED, capacity=5 * (wl["init_sheep"] + wl["init_wolves"]))
+    prev = st.stats()
+    for _ in range(warmup):
+        prev = st.step()
+    agent_steps, t0 = 0.0, time.perf_counter()
+    for _ in range(steps):
+        agent_steps += prev[0] + prev[1]
+        prev = st.step()
+    el = time.perf_counter() - t0
+    st.close()
+    return {"value": agent_steps / el, "ms_per_step": 1e3 * el / steps, "cores": 1,
+            "kind": "port", "sample": "iterations %d..%d, single-threaded oracle "
+            "(the reference's kernels unavailable)" % (warmup + 1, warmup + steps)}
+
+
+def kernel_traffic(name, cells, n_agents):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary
+    (profiles/ncu_traffic.json), scaled to this launch's cells and agents."""
+    tr = ncu_traffic().get(name)
+    if not tr:
+        return None
+    unit = tr.get("per")
+    if unit == "agent":
+        return tr["bytes_per_unit"] * n_agents
+    if unit == "cell+agent":
+        return tr["bytes_per_cell"] * cells + tr["bytes_per_agent"] * n_agents
+    if unit == "launch":
+        return tr["bytes_per_launch"]
+    return None
 
 
 def run_ours(args, dist):
@@ -273,24 +357,13 @@ def run_ours(args, dist):
     cells = p.grid_x * p.grid_y
     n_avg = prof_steps / prof_iters
     spec_b, P = spec_bytes_per_iter(cells, n_avg)
-    achieved = spec_b / ((tot_ms / launches) / 1e3) / 1e9
-    traffic = None
-    tr = ncu_traffic().get(name)
-    if tr:
-        unit = tr.get("per")
-        if unit == "agent":
-            traffic = tr["bytes_per_unit"] * n_avg
-        elif unit == "cell+agent":
-            traffic = tr["bytes_per_cell"] * cells + tr["bytes_per_agent"] * n_avg
-        elif unit == "launch":
-            traffic = tr["bytes_per_launch"]
+    launch_s = (tot_ms / launches) / 1e3
+    achieved = spec_b / launch_s / 1e9
+    traffic = kernel_traffic(name, cells, n_avg)
     step_bytes = sum(k[3] for k in kernels) / prof_iters
     step_ms = sum(k[2] for k in kernels) / prof_iters
     timed_spec_bytes = sum(spec_bytes_per_iter(cells, r.sheep + r.wolves)[0] for r in rows)
-    # algorithm-free lower bound: each cell's grass read and written and its
-    # cell offsets written and read once (12 B), each agent read and written
-    # once in and out (32 B)
-    timed_lb_bytes = sum(12.0 * cells + 32.0 * (r.sheep + r.wolves) for r in rows)
+    naive_bytes = sum(12.0 * cells + 32.0 * (r.sheep + r.wolves) for r in rows)
 
     # -- end to end through the C ABI with host buffers --
     dist.barrier()
@@ -311,13 +384,9 @@ def run_ours(args, dist):
         "n_gpus": dist.world, "steps": K, "warmup": W,
         "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic (model's own seeded init)",
-        "config": {"workload": wname, "grid": "%dx%d" % (p.grid_x, p.grid_y), "params": "v1",
-                   "init_sheep": p.init_sheep, "init_wolves": p.init_wolves,
-                   "seed": SEED, "agent_pool": cap, "state": "uint32 SoA agents, uint16 grass",
-                   "timed_iterations": "%d..%d" % (W + 1, W + K),
-                   "l2": "inputs larger than L2 (~2 GB working set)",
-                   "parallelism": "replicas" if dist.world > 1 else "single",
-                   "geometry": tuning if tuning else {"tile_cells": args.tile_cells}},
+        "config": config_of(args, dist.world),
+        "setup": {"agent_pool": cap, "state": "uint32 SoA agents, uint16 grass",
+                  "geometry": tuning if tuning else {"tile_cells": args.tile_cells}},
         "iters_per_s": iters_per_s,
         "e2e": {"value": e2e_value, "unit": "agent-steps/s",
                 "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
@@ -325,43 +394,94 @@ def run_ours(args, dist):
         "gpu_launches": None,
         "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "algorithmic_bytes_per_launch": spec_b,
+                     "traffic": traffic,
+                     "dram_achieved": traffic / launch_s / 1e9 if traffic else None,
+                     "dram_frac": traffic / launch_s / 1e9 / peak if traffic else None,
+                     "algorithmic_bytes_per_launch": spec_b,
                      "algorithmic_bytes": "12 C + (32 + 16 P) N, P = %d, N = %.0f" % (P, n_avg),
-                     "avg_launch_ms": tot_ms / launches},
+                     "avg_launch_ms": tot_ms / launches,
+                     "note": "frac: the reference-shaped step's bytes over the launch "
+                             "time; dram_frac: the kernel's measured DRAM bytes "
+                             "(traffic) over the same time"},
         "timed_roofline": {"algorithmic_bytes": timed_spec_bytes,
                            "achieved_gbs": timed_spec_bytes / (ms_max / 1e3) / 1e9,
                            "frac": timed_spec_bytes / (ms_max / 1e3) / 1e9 / peak,
                            "note": "same per-iteration figure over the K timed "
                                    "iterations and their whole device time"},
-        "lower_bound": {"bytes": timed_lb_bytes,
-                        "achieved_gbs": timed_lb_bytes / (ms_max / 1e3) / 1e9,
-                        "frac": timed_lb_bytes / (ms_max / 1e3) / 1e9 / peak,
-                        "note": "algorithm-free lower bound 12 C + 32 N per iteration "
-                                "over the K timed iterations"},
+        "naive_step": {"bytes": naive_bytes,
+                       "gbs_equivalent": naive_bytes / (ms_max / 1e3) / 1e9,
+                       "note": "12 C + 32 N per timed iteration: a step that streams "
+                               "every cell's grass and offsets and every agent in and "
+                               "out once; not a bound for this design, which reads "
+                               "only occupied cells' grass (kernel_bytes)"},
         "kernel_bytes": {"moved_bytes_per_step": step_bytes,
                          "kernel_ms_per_step": step_ms,
-                         "achieved_gbs": step_bytes / (step_ms / 1e3) / 1e9,
+                         "design_gbs": step_bytes / (step_ms / 1e3) / 1e9,
                          "note": "bytes the kernels must move in this design "
-                                 "(records in and out, occupied cells' grass)"},
-        "kernels": [{"name": k[0], "launches": k[1], "ms": k[2], "bytes": k[3],
-                     "gbs": (k[3] / (k[2] / 1e3) / 1e9) if k[2] > 0 else None}
+                                 "(records in and out, occupied cells' grass) over "
+                                 "their time; not a DRAM measurement"},
+        "kernels": [{"name": k[0], "launches": k[1], "ms": k[2], "design_bytes": k[3],
+                     "design_gbs": (k[3] / (k[2] / 1e3) / 1e9) if k[2] > 0 else None}
                     for k in kernels],
         "clocks": clk,
     }
     launches_per_iter = sum(k[1] for k in kernels) // prof_iters
     out["gpu_launches"] = K * launches_per_iter
+    if not args.no_full_run:
+        out["full_run"] = full_run(args, dist, p, cap)
     if args.batch_iters > 0:
         out["batched"] = batched_vs_plain(args, dist)
+    if dist.rank == 0 and not args.no_configs:
+        out["configs"] = run_configs(args, dist)["configs"]
+    if dist.rank == 0 and args.served_requests > 0:
+        out["served"] = run_served(args, dist)
     if dist.rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(args)
+        wl, _ = workload_dict(args)
+        r = cpu_sample(wl, args.cpu_steps, W)
+        out["cpu_baseline"] = {"value": r["value"], "unit": "agent-steps/s",
+                               "cores": r["cores"], "kind": r["kind"], "sample": r["sample"]}
     return out
+
+
+def full_run(args, dist, p, cap):
+    """The whole configured run (all its iterations) of the plain workload:
+    end to end through the C ABI (create, every iteration, every stats row
+    to the host, destroy) and device-timed (CUDA events over all
+    iterations, state resident)."""
+    import pphpc_gb300 as pp
+    dev = dist.local
+    kw = dict(device=dev, max_agents=cap, tile_cells=args.tile_cells,
+              autotune=args.tile_cells == 0)
+    dist.barrier()
+    t0 = time.perf_counter()
+    sim = pp.Simulation(p, SEED, **kw)
+    rows = [sim.stats0()] + sim.step(p.iters)
+    sim.close()
+    wall = dist.max(time.perf_counter() - t0)
+    steps = dist.sum(float(sum(r.sheep + r.wolves for r in rows[:-1])))
+    sim = pp.Simulation(p, SEED, **kw)
+    ms = dist.max(sim.time(p.iters))
+    sim.close()
+    n = [r.sheep + r.wolves for r in rows]
+    return {"iterations": p.iters, "agent_steps": steps,
+            "e2e_s": wall, "e2e_agent_steps_per_s": steps / wall,
+            "e2e_iters_per_s": p.iters / wall,
+            "device_ms": ms, "device_agent_steps_per_s": steps / (ms / 1e3),
+            "device_ms_per_iter": ms / p.iters,
+            "agents_first_last_peak": [n[0], n[-1], max(n)],
+            "peak_at_iteration": n.index(max(n)),
+            "includes": "e2e: pp_sim_create + %d iterations + %d stats rows to host "
+                        "+ destroy; device: CUDA events around the %d iterations"
+                        % (p.iters, p.iters + 1, p.iters)}
 
 
 def batched_vs_plain(args, dist):
     """The 64-run mix through pp_batch_run (one world) and run by run
     through pp_sim_* (one world per run), both end to end with host stats
-    buffers; aggregate agent-steps/s of each, and whether every run's stats
-    agree bit for bit."""
+    buffers; aggregate agent-steps/s of each, whether every run's stats
+    agree bit for bit, and the plain times per shape. The largest shape's
+    runs fill the GPU alone, so the plain time of that shape bounds what
+    batching can save."""
     import pphpc_gb300 as pp
     iters = args.batch_iters
     runs = []
@@ -383,19 +503,34 @@ def batched_vs_plain(args, dist):
     t0 = time.perf_counter()
     out_b = pp.batch_run(runs, pool_factor=POOL_FACTOR, device=dev, autotune=True)
     t1 = time.perf_counter()
-    out_p = []
+    out_p, t_p = [], []
     for p, sd in runs:
         n0 = p.init_sheep + p.init_wolves
+        ta = time.perf_counter()
         out_p.append(pp.run(p, sd, device=dev, max_agents=POOL_FACTOR * n0, autotune=True))
+        t_p.append(time.perf_counter() - ta)
     t2 = time.perf_counter()
     steps = 0
     exact = True
+    run_steps = []
     for rb, rp in zip(out_b, out_p):
-        steps += sum(r.sheep + r.wolves for r in rb[:-1])
+        st = sum(r.sheep + r.wolves for r in rb[:-1])
+        run_steps.append(st)
+        steps += st
         exact &= [r.as_tuple() for r in rb] == [r.as_tuple() for r in rp]
     tb = dist.max(t1 - t0)
     tp = dist.max(t2 - t1)
     steps_all = dist.sum(float(steps))
+    shapes, k = [], 0
+    for side, version, n in MIX:
+        st = float(sum(run_steps[k:k + n]))
+        sec = float(sum(t_p[k:k + n]))
+        shapes.append({"shape": "%dx%d v%d" % (side, side, version), "runs": n,
+                       "agent_steps": st, "plain_s": sec,
+                       "plain_agent_steps_per_s": st / sec if sec > 0 else None,
+                       "share_of_agent_steps": st / max(steps, 1)})
+        k += n
+    big = max(shapes, key=lambda d: d["agent_steps"])
     return {"runs": len(runs), "iterations": iters,
             "mix": "32x200^2 v1, 16x800^2 v2, 8x1600^2 v1, 8x3200^2 v2, seeds 100..163",
             "agent_steps": steps_all,
@@ -403,9 +538,19 @@ def batched_vs_plain(args, dist):
             "batched_agent_steps_per_s": steps_all / tb,
             "plain_agent_steps_per_s": steps_all / tp,
             "speedup": tp / tb, "bit_exact_batched_vs_plain": bool(exact),
+            "per_shape_plain": shapes,
+            "largest_shape": big["shape"],
+            "largest_shape_share": big["share_of_agent_steps"],
+            "speedup_if_small_runs_free": tp / big["plain_s"],
+            "speedup_at_batched_rate_if_small_runs_free":
+                tp / (big["agent_steps"] / (steps_all / tb)),
+            "speedup_bound_note": "the largest shape's runs fill the GPU alone; with every "
+                                  "other run free, the plain time would fall to theirs "
+                                  "(speedup_if_small_runs_free), or to their agent-steps at "
+                                  "the batched world's own rate",
             "geometry_batched": tune_b,
-            "geometry_plain": {"%dx%d %s" % (k[0], k[0], "v1" if k[1] == 4 else "v2"): v
-                               for k, v in tune_p.items()},
+            "geometry_plain": {"%dx%d %s" % (k_[0], k_[0], "v1" if k_[1] == 4 else "v2"): v
+                               for k_, v in tune_p.items()},
             "timing": "wall clock, end to end through the C ABI (create, "
                       "iterations, stats rows to host, destroy)"}
 
@@ -413,10 +558,10 @@ def batched_vs_plain(args, dist):
 def run_configs(args, dist):
     """The reference's two small plain configs (100^2 v1 seed 0 and 400^2
     v2 seed 1, 4000 iterations), each run whole on the GPU (end to end
-    through pp_sim_*, tuned geometry) and by the CPU restatement of the
-    reference's CPU algorithm on all host threads."""
+    through pp_sim_*, tuned geometry) and by the reference's CPU kernels
+    on all host threads."""
     import pphpc_gb300 as pp
-    from oracle import cpu_port
+    from oracle import pp_ref
     if dist.rank != 0:
         return None
     out = {"workload": "configs", "metric": "agent-steps/s", "unit": "agent-steps/s",
@@ -429,17 +574,21 @@ def run_configs(args, dist):
         rows = pp.run(p, seed, device=dist.local, max_agents=POOL_FACTOR * n0, autotune=True)
         tg = time.perf_counter() - t0
         steps_g = sum(r.sheep + r.wolves for r in rows[:-1])
-        t0 = time.perf_counter()
-        crow = cpu_port.run(p, seed)
-        tc = time.perf_counter() - t0
-        steps_c = float(crow[:-1, 0].sum() + crow[:-1, 1].sum())
-        out["configs"].append({
-            "config": "%dx%d v%d seed %d, 4000 iterations" % (side, side, version, seed),
-            "gpu_agent_steps_per_s": steps_g / tg, "gpu_iters_per_s": 4000 / tg,
-            "cpu_agent_steps_per_s": steps_c / tc, "cpu_iters_per_s": 4000 / tc,
-            "cpu_cores": cpu_port.threads(), "cpu_kind": "port",
-            "timing": "wall clock of the whole run (GPU: create, 4000 iterations, "
-                      "stats to host, destroy)"})
+        c = {"config": "%dx%d v%d seed %d, 4000 iterations" % (side, side, version, seed),
+             "gpu_agent_steps_per_s": steps_g / tg, "gpu_iters_per_s": 4000 / tg,
+             "timing": "wall clock of the whole run (GPU: create, 4000 iterations, "
+                       "stats to host, destroy; CPU: create, init, 4000 iterations)"}
+        if pp_ref.available():
+            t0 = time.perf_counter()
+            crow = pp_ref.run(p, seed)
+            tc = time.perf_counter() - t0
+            steps_c = float(crow[:-1, 0].sum() + crow[:-1, 1].sum())
+            s_ = pp_ref.Sim(p, seed, 1)
+            cores = s_.threads()
+            s_.close()
+            c.update(cpu_agent_steps_per_s=steps_c / tc, cpu_iters_per_s=4000 / tc,
+                     cpu_cores=cores, cpu_kind="reference")
+        out["configs"].append(c)
     return out
 
 
@@ -496,36 +645,32 @@ def run_served(args, dist):
             "agent_steps": steps, "wall_s": wall,
             "agent_steps_per_s": steps / wall, "unit": "s",
             "higher_is_better": False, "n_gpus": 1,
+            "last_arrival_s": reqs[-1][0],
             "config": {"workload": "served: Poisson 20/s, side in {100..3200}, "
                                    "v1/v2 p=0.5, iters U[500,4000], 150 GB budget"}}
 
 
-def cpu_baseline(args):
-    from oracle import cpu_port
-    return cpu_port.baseline_sample(WORKLOAD, SEED, iters=args.cpu_iters)
-
-
 def run_reference(args, dist):
+    """The reference's own CPU algorithm on the workload and window of the
+    GPU arm, rank 0 only."""
     if dist.rank != 0:
         return None
-    from oracle import cpu_port
-    wl, wname = dict(WORKLOAD), WORKLOAD_NAME
-    if args.side != 12800:
-        a = args.side * args.side
-        wl.update(grid_x=args.side, grid_y=args.side, init_sheep=a * 4 // 100,
-                  init_wolves=a * 2 // 100)
-        wname = "pphpc-%dx%d-v1" % (args.side, args.side)
-    r = cpu_port.run_steps(wl, SEED, args.steps, args.warmup)
+    from oracle import pp_ref
+    wl, _ = workload_dict(args)
+    if not pp_ref.available():
+        return {"impl": "reference",
+                "unavailable": "the reference's CPU kernels could not be built "
+                               "(no reference tree and no preprocessed copy)"}
+    r = cpu_sample(wl, args.steps, args.warmup)
     return {
         "impl": "reference", "metric": "agent-steps/s", "value": r["value"],
         "unit": "agent-steps/s", "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic (model's own seeded init)",
-        "config": {"workload": wname, "grid": "%dx%d" % (wl["grid_x"], wl["grid_y"]),
-                   "params": "v1", "seed": SEED},
+        "config": config_of(args, dist.world),
         "cpu_baseline": {"value": r["value"], "unit": "agent-steps/s",
-                         "cores": r["cores"], "kind": "port", "sample": r["sample"]},
+                         "cores": r["cores"], "kind": r["kind"], "sample": r["sample"]},
         "e2e": {"value": r["value"], "unit": "agent-steps/s",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -537,12 +682,16 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--cpu-iters", type=int, default=2)
+    ap.add_argument("--cpu-steps", type=int, default=10,
+                    help="timed iterations of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-full-run", action="store_true")
+    ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--batch-iters", type=int, default=4000,
                     help="iterations per run of the batched-vs-plain mix (0 = skip)")
     ap.add_argument("--workload", choices=["plain", "served", "configs"], default="plain")
-    ap.add_argument("--served-requests", type=int, default=1000)
+    ap.add_argument("--served-requests", type=int, default=1000,
+                    help="requests of the served stream (0 = skip the leg)")
     ap.add_argument("--side", type=int, default=12800,
                     help="grid side of the plain workload (agents scale by area)")
     ap.add_argument("--tile-cells", type=int, default=0,

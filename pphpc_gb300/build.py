@@ -111,10 +111,11 @@ def build_oracle():
 def build_all(verbose=False):
     lib = build_library(verbose=verbose)
     build_oracle()
-    # the CPU restatement of the reference's algorithm (test infrastructure)
+    # the reference's own CPU kernels (test and baseline infrastructure),
+    # when the reference tree or its preprocessed kernels are present
     sys.path.insert(0, ROOT)
-    from oracle import cpu_port
-    cpu_port.build()
+    from oracle.ref import build_ref
+    build_ref.build()
     return lib
 
 

@@ -99,9 +99,20 @@ def compare(fm_a, fm_b, alpha=0.05):
     return passed, table
 
 
+def raw_below(table, alpha=0.05):
+    """Number of measures whose uncorrected p-value is below alpha. With 36
+    measures and no difference about 36 x 0.05 = 1.8 are expected by chance
+    (more spread than a binomial, because the measures are correlated)."""
+    return sum(1 for t in table if t[3] < alpha)
+
+
 def format_table(table):
     lines = ["%-16s %-7s %-13s %9s %9s %14s %14s" % (
         "output", "measure", "test", "p", "p_holm", "mean_a", "mean_b")]
     for t in table:
         lines.append("%-16s %-7s %-13s %9.4f %9.4f %14.4f %14.4f" % t)
+    lines.append("uncorrected p < 0.05: %d of %d measures (about %.1f expected "
+                 "by chance); smallest Holm-adjusted p: %.4f"
+                 % (raw_below(table), len(table), 0.05 * len(table),
+                    min(t[4] for t in table)))
     return "\n".join(lines)
