@@ -491,10 +491,13 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 		};
 
 		/* ---- E1: move draws of the outputs, per-class counts; with room in
-		 * the cell counters' words (2 act_cap <= T), each output's key bits and
-		 * class are kept for E2, else only its direction ---- */
+		 * the cell counters' words (2 act_cap <= T) and offsets that fit 10
+		 * bits (2 act_cap <= 1024), each output's cell in its destination
+		 * tile (bits 0-12), direction (13-15), class (16-21) and offset in its
+		 * class's group (22-31) are kept for E2, else only its direction ---- */
 		bool bad = false;
-		const bool cache = in_smem && 2u * w.act_cap <= (uint32_t) (CPT * NT);
+		const bool cache = in_smem && 2u * w.act_cap <= (uint32_t) (CPT * NT)
+			&& 2u * w.act_cap <= 1024u;
 		uint32_t *DEST = scnt;
 		for (uint32_t o = tid; o < total; o += NT) {
 			uint32_t j, nb, en, rank;
@@ -519,9 +522,9 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 				bad = true;
 				cls = NCLS;                      /* counted nowhere */
 			}
-			if (cache) DEST[o] = klo | (code << REC_DIR_SHIFT) | (cls << 16);
+			const uint32_t off = warp_agg_add(s_ccnt, cls);
+			if (cache) DEST[o] = klo | (code << REC_DIR_SHIFT) | (cls << 16) | (off << 22);
 			else DIR[o] = (uint8_t) code;
-			warp_agg_add(s_ccnt, cls);
 		}
 		if (bad) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
 		__syncthreads();
@@ -569,10 +572,10 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 				if (cache) {
 					const uint32_t d = DEST[o];
 					const uint32_t code = (d >> REC_DIR_SHIFT) & 7u;
-					cls = d >> 16;
+					cls = (d >> 16) & 63u;
 					key = (d & 0xffffu) | (rank << REC_RANK_SHIFT);
 					val = code >= DIR_PARKED ? (tb | en) : (tb | ((en - 1) & run.emask));
-					const uint32_t pos = warp_agg_add(s_cpos, cls);
+					const uint32_t pos = s_cpos[cls] + (d >> 22);
 					if (cls != NCLS) {
 						kGo[pos] = key;
 						vGo[pos] = val;
