@@ -1,14 +1,18 @@
 """Statistical parity of the CUDA path with the reference's own CPU
 algorithm (opencl/pp/pp_cpu.cl compiled unmodified, on all host threads;
-only its RNG is a stand-in): 30 GPU replications (one batched world) against
-30 CPU replications, PPHPC focal measures of the six outputs, alpha = 0.05
-family-wise (Holm), with the count of uncorrected p < 0.05 reported."""
+only its RNG is a stand-in): per configuration, 30 GPU replications (one
+batched world) against 30 CPU replications, PPHPC focal measures of the six
+outputs. The family is the whole suite (4 configurations x 36 measures):
+Holm correction over its 144 p-values at alpha = 0.05, so that the suite
+fails on identical implementations 5% of the time rather than about 19%
+(four families at 5% each). Per configuration, the count of uncorrected
+p < 0.05 (about 1.8 of 36 expected by chance) is reported and bounded."""
 import numpy as np
 import pytest
 
 import pphpc_gb300 as pp
 from common import params
-from focal import compare, focal_measures, format_table, raw_below
+from focal import compare, focal_measures, format_table, holm, raw_below
 from oracle import pp_ref
 
 pytestmark = [pytest.mark.gpu,
@@ -17,6 +21,7 @@ pytestmark = [pytest.mark.gpu,
 
 REPS = 30
 SS_FROM = 1000
+CONFIGS = [(100, 1, 8), (200, 2, 40), (400, 2, 40), (800, 1, 8)]   # side, version, pool
 
 
 def _gpu_fms(p, seeds, pool_factor):
@@ -30,13 +35,21 @@ def _ref_fms(p, seeds):
                      for s in seeds])
 
 
-@pytest.mark.parametrize("side,version,pool_factor", [
-    (100, 1, 8), (200, 2, 40), (400, 2, 40), (800, 1, 8)])
-def test_gpu_vs_reference_cpu(side, version, pool_factor):
-    p = params(side, version, iters=4000)
-    a = _gpu_fms(p, range(REPS), pool_factor)
-    b = _ref_fms(p, range(7000, 7000 + REPS))
-    ok, table = compare(a, b)
-    print("\n%dx%d v%d\n" % (side, side, version) + format_table(table))
-    assert ok, format_table(table)
-    assert raw_below(table) <= 8, format_table(table)
+def test_gpu_vs_reference_cpu():
+    tables = []
+    for side, version, pool_factor in CONFIGS:
+        p = params(side, version, iters=4000)
+        a = _gpu_fms(p, range(REPS), pool_factor)
+        b = _ref_fms(p, range(7000, 7000 + REPS))
+        _, table = compare(a, b)
+        print("\n%dx%d v%d\n" % (side, side, version) + format_table(table))
+        tables.append(("%dx%d v%d" % (side, side, version), table))
+    raw = [t[3] for _, table in tables for t in table]
+    adj = holm(raw)
+    worst = int(np.argmin(adj))
+    name, table = tables[worst // 36]
+    print("\nsuite: smallest Holm-adjusted p over %d measures: %.4f (%s, %s %s)"
+          % (len(raw), adj[worst], name, table[worst % 36][0], table[worst % 36][1]))
+    assert adj.min() >= 0.05, (name, table[worst % 36])
+    for name, table in tables:
+        assert raw_below(table) <= 8, name + "\n" + format_table(table)
