@@ -112,15 +112,6 @@ __device__ __forceinline__ uint32_t warp_agg_add(uint32_t *ctr, uint32_t key)
 	return base + __popc(peers & ((1u << lane) - 1));
 }
 
-/* Canonical order of the agents of one destination cell (x, y): by source
- * cell, then by rank in the source cell's list. */
-__device__ __forceinline__ int64_t order_key(uint32_t rec, uint32_t x,
-	uint32_t y, uint32_t gx, uint32_t gy)
-{
-	const int32_t off = src_offset((rec >> REC_DIR_SHIFT) & 7u, x, y, gx, gy);
-	return (int64_t) off * 65536 + (rec >> REC_RANK_SHIFT);
-}
-
 /* Exclusive scan of one value per thread over the NT threads of the CTA;
  * the total goes to *total. */
 template <int NT>
@@ -371,10 +362,24 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 				if (e - b > 1) {
 					const uint32_t lr = lt0 + c;
 					const uint32_t y = fastdiv_div(lr, run.gxdiv), x = lr - y * run.gx;
-					const int64_t kx = order_key(rk, x, y, run.gx, run.gy);
+					/* the cell's four neighbour offsets, then each mate's
+					 * key (source cell offset, rank in the source list)
+					 * with selects rather than a switch on its arrival
+					 * direction, so the lanes of a warp do not diverge */
+					const int32_t o1 = src_offset(1, x, y, run.gx, run.gy);
+					const int32_t o2 = src_offset(2, x, y, run.gx, run.gy);
+					const int32_t o3 = src_offset(3, x, y, run.gx, run.gy);
+					const int32_t o4 = src_offset(4, x, y, run.gx, run.gy);
+					auto okey = [&](uint32_t rec) {
+						const uint32_t dr = (rec >> REC_DIR_SHIFT) & 7u;
+						const int32_t off = dr == 1 ? o1 : dr == 2 ? o2 : dr == 3 ? o3
+							: dr == 4 ? o4 : 0;
+						return (int64_t) off * 65536 + (rec >> REC_RANK_SHIFT);
+					};
+					const int64_t kx = okey(rk);
 					d = b;
 					for (uint32_t q = b; q < e; q++)
-						d += order_key(UK[PERM[q]], x, y, run.gx, run.gy) < kx;
+						d += okey(UK[PERM[q]]) < kx;
 				}
 				if (d - b > 0xffffu) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
 				LK[d] = c | (d - b) << 16;
