@@ -157,3 +157,58 @@ def timed_steps(p, seed, steps, warmup, max_agents=0, threads=0):
     return {"value": agent_steps / total, "ms_per_step": 1e3 * total / steps,
             "agent_steps": agent_steps, "seconds": total, "cores": threads_used,
             "setup_s": t_init}
+
+
+_lib_noshuf = None
+
+
+def lib_noshuf():
+    """The reference's kernels with the in-cell shuffle compiled out."""
+    global _lib_noshuf
+    if _lib_noshuf is None:
+        from oracle.ref import build_ref
+        path = build_ref.build(noshuf=True)
+        if path is None:
+            raise Unavailable("the reference tree and its preprocessed kernels "
+                              "are both absent")
+        L = C.CDLL(path)
+        u16p, u8p = C.POINTER(C.c_uint16), C.POINTER(C.c_uint8)
+        L.ppr_step2_cells.restype = C.c_int
+        L.ppr_step2_cells.argtypes = [_u32p, C.c_uint32, _u32p, u16p, u8p, _u32p,
+                                      C.c_uint32, u16p, u8p, _u32p, _u32p, _u32p]
+        _lib_noshuf = L
+    return _lib_noshuf
+
+
+def step2_cells(p, cell_of, energy, typ, grass):
+    """One run of the reference's step2 kernel (shuffle compiled out) over a
+    grid_x x 3 grid: agent i in cell cell_of[i] (list order = array order)
+    with energy[i] (u16) and type typ[i]; grass: 3 grid_x countdowns.
+    Returns (per-cell lists of (energy, type) after the step, grass after,
+    the stats row of 7 uint32)."""
+    prm = _params(p)
+    cell_of = np.ascontiguousarray(cell_of, np.uint32)
+    energy = np.ascontiguousarray(energy, np.uint16)
+    typ = np.ascontiguousarray(typ, np.uint8)
+    grass = np.ascontiguousarray(grass, np.uint32)
+    ncell = len(grass)
+    cap = 3 * len(cell_of) + 16
+    oe = np.zeros(cap, np.uint16)
+    ot = np.zeros(cap, np.uint8)
+    cnt = np.zeros(ncell, np.uint32)
+    gout = np.zeros(ncell, np.uint32)
+    st = np.zeros(7, np.uint32)
+    u16p, u8p = C.POINTER(C.c_uint16), C.POINTER(C.c_uint8)
+    rc = lib_noshuf().ppr_step2_cells(
+        prm, len(cell_of), cell_of.ctypes.data_as(_u32p), energy.ctypes.data_as(u16p),
+        typ.ctypes.data_as(u8p), grass.ctypes.data_as(_u32p), cap,
+        oe.ctypes.data_as(u16p), ot.ctypes.data_as(u8p), cnt.ctypes.data_as(_u32p),
+        gout.ctypes.data_as(_u32p), st.ctypes.data_as(_u32p))
+    if rc != 0:
+        raise RuntimeError("reference step2 harness failed (%d)" % rc)
+    lists, o = [], 0
+    for c in range(ncell):
+        k = int(cnt[c])
+        lists.append(list(zip(oe[o:o + k].tolist(), ot[o:o + k].tolist())))
+        o += k
+    return lists, gout, st

@@ -15,7 +15,10 @@ reference tree, as C++ for the host:
      into oracle/_ref/pp_cpu_kernels.ii (needs the reference tree);
   2. compile that translation unit with oracle/ref/pp_cpu_host.cpp (the
      reference host's work sizes and launch loop, with OpenMP threads as
-     work items) into oracle/_ref/libpp_cpu_ref.so.
+     work items) into oracle/_ref/libpp_cpu_ref.so;
+  3. the same with the in-cell shuffle compiled out (-DMAX_AGENT_SHUF=1, the
+     reference's own switch) into oracle/_ref/libpp_cpu_ref_noshuf.so, for
+     the test that pins the oracle's actions to the reference's step2.
 
 oracle/_ref/ is not committed. Where the reference tree is absent (a GPU
 host gets a copy of this working tree without it), step 1 is skipped and the
@@ -38,6 +41,11 @@ COMPAT = os.path.join(HERE, "ocl_compat.hpp")
 HOST = os.path.join(HERE, "pp_cpu_host.cpp")
 II = os.path.join(OUT, "pp_cpu_kernels.ii")
 LIB = os.path.join(OUT, "libpp_cpu_ref.so")
+# the same kernels with the in-cell shuffle compiled out (MAX_AGENT_SHUF 1,
+# the reference's own switch, pp_cpu.cl:640): a cell's list order is then
+# its acting order, which the act pin test sets
+II_NOSHUF = os.path.join(OUT, "pp_cpu_kernels_noshuf.ii")
+LIB_NOSHUF = os.path.join(OUT, "libpp_cpu_ref_noshuf.so")
 CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-Wall"]
 
 
@@ -58,23 +66,36 @@ def _run(cmd):
         raise RuntimeError("build failed: %s\n%s" % (" ".join(cmd), p.stdout))
 
 
-def build():
-    """Build oracle/_ref/libpp_cpu_ref.so; returns its path, or None when
-    neither the reference tree nor a preprocessed copy is available."""
-    sys.path.insert(0, os.path.dirname(ORACLE))
+def _build_one(ii, lib, defines):
     from pphpc_gb300.build import native_ok
-    os.makedirs(OUT, exist_ok=True)
     src = os.path.join(reference_root(), "opencl", "pp")
     cl = [os.path.join(src, "pp_common.cl"), os.path.join(src, "pp_cpu.cl")]
     if all(os.path.exists(f) for f in cl):
-        if _stale(II, [KERNELS, COMPAT] + cl):
-            _run(["g++"] + CXXFLAGS + ["-E", "-P", "-I", src, KERNELS, "-o", II])
-    elif not os.path.exists(II):
+        if _stale(ii, [KERNELS, COMPAT] + cl):
+            _run(["g++"] + CXXFLAGS + defines + ["-E", "-P", "-I", src, KERNELS, "-o", ii])
+    elif not os.path.exists(ii):
         return None
-    if _stale(LIB, [II, HOST]) or not native_ok(LIB):
-        _run(["g++"] + CXXFLAGS + ["-shared", "-fopenmp", II, HOST, "-o", LIB])
-    return LIB
+    if _stale(lib, [ii, HOST]) or not native_ok(lib):
+        _run(["g++"] + CXXFLAGS + ["-shared", "-fopenmp", ii, HOST, "-o", lib])
+    return lib
+
+
+def build(noshuf=False):
+    """Build oracle/_ref/libpp_cpu_ref.so (or, with noshuf, the variant with
+    the in-cell shuffle compiled out); returns its path, or None when
+    neither the reference tree nor a preprocessed copy is available."""
+    sys.path.insert(0, os.path.dirname(ORACLE))
+    os.makedirs(OUT, exist_ok=True)
+    if noshuf:
+        return _build_one(II_NOSHUF, LIB_NOSHUF, ["-DMAX_AGENT_SHUF=1"])
+    return _build_one(II, LIB, [])
+
+
+def build_all():
+    lib = build()
+    build(noshuf=True)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build())
+    print(build_all())

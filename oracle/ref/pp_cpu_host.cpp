@@ -233,6 +233,77 @@ int ppr_step(ppr_sim *s, uint32_t n, uint32_t *rows)
 
 int ppr_threads(const ppr_sim *s) { return s->threads; }
 
+/* The reference's agent and cell records as its kernels lay them out
+ * (pp_cpu.cl:60-110): energy u16, type u8, action u8, next u32; grass u32,
+ * first agent u32. */
+struct ref_agent { uint16_t energy; uint8_t type, action; uint32_t next; };
+struct ref_cell { uint32_t grass, first; };
+
+/* Runs the reference's step2 kernel (actions and stats) once, for iteration
+ * 1, over a grid of grid_x x 3 cells (one work item, three turns) whose
+ * cells hold given agent lists. Agent i sits in cell cell_of[i] with
+ * energy[i] and type[i] (0 sheep, 1 wolf), having moved (action flag set,
+ * as step1 leaves it); a cell's list holds its agents in array order.
+ * grass_in/grass_out are the 3 grid_x countdowns. On return, out_energy /
+ * out_type hold every cell's list after the step, cell by cell in list
+ * order (at most max_out entries), out_count[c] the length of cell c's list,
+ * and stats7 the step's stats row (sheep, wolves, grass, sheep_en,
+ * wolves_en, grass_en, errors). With the kernels compiled with shuffling
+ * off (MAX_AGENT_SHUF 1) the list order is the acting order, so a test can
+ * set the outcome of every draw by using reproduction probabilities of 0
+ * or 100. Returns 0, -2 (params[10] is not 3 or grid_x differs), -3 (no
+ * memory) or -8 (more than max_out agents after the step). */
+int ppr_step2_cells(const uint32_t *params, uint32_t n, const uint32_t *cell_of,
+	const uint16_t *energy, const uint8_t *type, const uint32_t *grass_in,
+	uint32_t max_out, uint16_t *out_energy, uint8_t *out_type,
+	uint32_t *out_count, uint32_t *grass_out, uint32_t *stats7)
+{
+	if (params[10] != 3 || ppr_sizeof_agent() != sizeof(ref_agent)
+		|| ppr_sizeof_cell() != sizeof(ref_cell))
+		return -2;
+	ppr_sim s{};
+	memcpy(s.params, params, sizeof(s.params));
+	s.max_agents = 1u << 22;
+	s.max_iters = 1;
+	s.gws = 1;
+	s.rpw = 3;
+	const uint32_t cells = params[9] * 3;
+	std::vector<ref_agent> agents(s.max_agents);
+	std::vector<ref_cell> cl(cells);
+	std::vector<uint32_t> stats(7 * 2, 0);
+	uint64_t seed = 0x5EED;
+	if (n >= s.max_agents) return -8;
+	for (uint32_t c = 0; c < cells; c++) {
+		cl[c].grass = grass_in[c];
+		cl[c].first = 0xffffffffu;
+	}
+	for (uint32_t k = n; k-- > 0;) {
+		ref_agent &a = agents[k];
+		a.energy = energy[k];
+		a.type = type[k];
+		a.action = 1;
+		a.next = cl[cell_of[k]].first;
+		cl[cell_of[k]].first = k;
+	}
+	set_constants(&s);
+	for (unsigned t = 0; t < 3; t++)
+		ppr_kernel_step2(agents.data(), cl.data(), &seed, stats.data(), 1, t, 0, 1);
+	uint32_t o = 0;
+	for (uint32_t c = 0; c < cells; c++) {
+		uint32_t k = 0;
+		for (uint32_t a = cl[c].first; a != 0xffffffffu; a = agents[a].next, k++) {
+			if (o >= max_out) return -8;
+			out_energy[o] = agents[a].energy;
+			out_type[o] = agents[a].type;
+			o++;
+		}
+		out_count[c] = k;
+		grass_out[c] = cl[c].grass;
+	}
+	memcpy(stats7, stats.data() + 7, 7 * sizeof(uint32_t));
+	return 0;
+}
+
 /* A whole run: iters iterations (the parameter file's own when 0), stats
  * rows 0..iters into stats_out ((iters + 1) x 7 uint32). Returns ppr_create's
  * codes. */

@@ -115,7 +115,7 @@ def build_all(verbose=False):
     # when the reference tree or its preprocessed kernels are present
     sys.path.insert(0, ROOT)
     from oracle.ref import build_ref
-    build_ref.build()
+    build_ref.build_all()
     return lib
 
 
