@@ -2,10 +2,10 @@
  * pp_oracle.c -- single-threaded CPU restatement of the PPHPC step.
  *
  * TEST INFRASTRUCTURE ONLY (the checker for the CUDA path; never linked by
- * the product). Parity unpinned against the reference itself: the reference
- * has no tests or golden vectors and its cl_ops RNG is not in the tree, so
- * this file restates the model rules with Philox draws; see pp_oracle.h for
- * the reference lines each phase follows.
+ * the product). The reference has no tests or golden vectors and its cl_ops
+ * RNG is not in the tree, so this file restates the model rules with
+ * Philox draws; pp_oracle.h gives the reference lines each phase follows
+ * and how the oracle is pinned to the reference's own CPU kernels.
  *
  * State: every cell holds an ordered list of agents; stored as an array
  * stably sorted by cell (the initial agents are listed in creation order).

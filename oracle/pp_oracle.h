@@ -7,9 +7,14 @@
  *
  * Parity status: the reference (nunofachada/pphpc) ships no tests, golden
  * vectors or known-answer files, and its RNG (cl_ops, unpinned) is not in
- * the reference tree. Bit-exact parity is therefore defined against this
- * oracle, which implements the reference's model rules with Philox4x32-10
- * draws; agreement with the reference's own CPU algorithm is statistical.
+ * the reference tree, so whole runs cannot match the reference draw for
+ * draw. This oracle implements the reference's model rules with
+ * Philox4x32-10 draws and is pinned to the reference's own CPU kernels
+ * (opencl/pp/pp_cpu.cl, compiled unmodified for the host by
+ * oracle/ref/build_ref.py): its in-cell actions bit for bit wherever the
+ * draws' outcomes can be fixed (tests/test_ref_act_pin.py), its whole
+ * dynamics statistically (tests/test_stats_parity.py). The CUDA path is
+ * checked bit for bit against this oracle.
  *
  * Rules followed (paths relative to the pphpc project root):
  *   init grass      opencl/pp/pp_gpu.cl:368-398, netlogo/pphpc.nlogo:27-35

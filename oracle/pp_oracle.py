@@ -2,8 +2,9 @@
 
 TEST INFRASTRUCTURE ONLY: the checker for the CUDA path. Only tests/,
 __graft_entry__.smoke() and bench.py's CPU-baseline leg may import this.
-Parity unpinned against the reference itself (it ships no tests or golden
-vectors and its cl_ops RNG is absent); see pp_oracle.h.
+It is pinned to the reference's own CPU kernels (its actions bit for bit
+where the draws' outcomes can be fixed, its dynamics statistically); see
+pp_oracle.h.
 """
 import ctypes as C
 import os
