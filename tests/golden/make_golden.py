@@ -20,6 +20,9 @@ made with `python tests/golden/make_golden.py large [name ...]`):
       and the SHA-256 of the canonical state after iteration 300 (agents'
       cells and type|energy words, then the grass countdowns, as the
       oracle lists them);
+  stats_12800v1_s2_full.npz  the same run for all 4000 iterations (several
+      hours of one core); written every 250 iterations, so a file from an
+      interrupted run holds rows 0..k and `iters_done` = k;
   stats_mix_<side>v<v>_s<seed>.npz  all 4001 rows of one run of each class
       of the 64-run batched mix: 200x200 v1 seed 100, 800x800 v2 seed 132,
       1600x1600 v1 seed 148, 3200x3200 v2 seed 156 (the mix's first run of
@@ -94,7 +97,28 @@ def state_digest(cell, en, grass):
     return h.hexdigest()
 
 
+def make_full_12800(name="12800v1_s2_full", every=250):
+    d, seed, _, pool = LARGE["12800v1_s2_r300"]
+    iters = d["iters"]
+    st = orc.State(d, seed, capacity=pool)
+    rows = [st.stats()]
+    path = os.path.join(HERE, "stats_%s.npz" % name)
+    for k in range(1, iters + 1):
+        rows.append(st.step())
+        if k % every == 0 or k == iters:
+            tmp = path + ".tmp.npz"
+            np.savez_compressed(tmp, rows=np.array(rows, np.uint64),
+                                params=np.array([d[f] for f in FIELDS], np.uint32),
+                                seed=np.array([seed], np.uint64),
+                                pool=np.array([pool], np.uint64),
+                                iters_done=np.array([k], np.uint64))
+            os.replace(tmp, path)
+    st.close()
+
+
 def make_large(name):
+    if name == "12800v1_s2_full":
+        return make_full_12800()
     d, seed, iters, pool = LARGE[name]
     st = orc.State(d, seed, capacity=pool)
     rows = [st.stats()]
@@ -141,7 +165,7 @@ def main():
 
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "large":
-        for n in sys.argv[2:] or sorted(LARGE):
+        for n in sys.argv[2:] or sorted(LARGE) + ["12800v1_s2_full"]:
             make_large(n)
     else:
         main()
