@@ -105,3 +105,18 @@ def test_served_world_holds_mix_classes():
         assert ev.done == 1 and ev.status == 0
         assert first_diff(rows_array(srv.read(rid)), want) is None, rid
     srv.close()
+
+
+def test_12800_full_run_rows():
+    """The 12800x12800 v1 workload (seed 2, pool 5x) against every row the
+    oracle's full-length fixture holds (all 4000 iterations, or the first
+    rows of an interrupted generation)."""
+    path = os.path.join(GOLDEN, "stats_12800v1_s2_full.npz")
+    if not os.path.exists(path):
+        pytest.skip("full-length fixture not generated (make_golden.py large)")
+    g, p, seed = _fixture("12800v1_s2_full")
+    want = g["rows"]
+    k = int(g["iters_done"][0])
+    assert len(want) == k + 1 and k >= 500
+    got = rows_array(pp.run(p, seed, k, max_agents=int(g["pool"][0])))
+    assert first_diff(got, want) is None
