@@ -286,6 +286,27 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 			const uint32_t *kGi = pin ? w.kG1 : w.kG0;
 			const uint32_t *vGi = pin ? w.vG1 : w.vG0;
 			const uint32_t m_up = (m + NT - 1) / NT * NT;   /* warp-uniform trip count */
+			if (m <= NT) {
+				/* one item per thread: one group search instead of two */
+				const uint32_t j = tid;
+				uint32_t lo = 0, hi = max(nin, 1u);
+#pragma unroll
+				for (int step = 0; step < 5; step++) {
+					const uint32_t mid = (lo + hi) >> 1;
+					const uint32_t pm = __shfl_sync(0xffffffffu, grp_pref, mid);
+					if (hi - lo > 1) {
+						if (pm <= j) lo = mid; else hi = mid;
+					}
+				}
+				const uint32_t src = __shfl_sync(0xffffffffu, grp_start, lo)
+					+ (j - __shfl_sync(0xffffffffu, grp_pref, lo));
+				if (j < m) {
+					const uint32_t kk = kGi[src], vv = vGi[src];
+					UK[j] = kk;
+					UV[j] = vv;
+					atomicAdd(&scnt[SLOT(kk & lcmask)], 1u);
+				}
+			} else
 			for (uint32_t j0 = tid; j0 < m_up; j0 += 2 * NT) {
 				uint32_t src[2];
 #pragma unroll
@@ -622,7 +643,16 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 			const uint32_t wid = tid >> 5;
 			const uint32_t sw = warp_sum(sheep | (wolves << 16));
 			const uint32_t ew = warp_sum(eats);
-			const uint64_t se = warp_sum(sen), we = warp_sum(wen);
+			/* energy sums: one 32-bit warp reduction each while every
+			 * lane's sum is below 2^26 (32 of them stay below 2^31) */
+			uint64_t se, we;
+			if (__all_sync(0xffffffffu, ((sen | wen) >> 26) == 0)) {
+				se = __reduce_add_sync(0xffffffffu, (uint32_t) sen);
+				we = __reduce_add_sync(0xffffffffu, (uint32_t) wen);
+			} else {
+				se = warp_sum(sen);
+				we = warp_sum(wen);
+			}
 			if (lane == 0) {
 				red[0][wid] = sw & 0xffffu;
 				red[1][wid] = sw >> 16;
