@@ -65,3 +65,13 @@ def test_reference_arm_under_torchrun_prints_one_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["config"]["grid"] == "200x200"
+    # the reference's own CPU kernels, when they build here
+    sys.path.insert(0, ROOT)
+    from oracle import pp_ref
+    if pp_ref.available():
+        assert d["cpu_baseline"]["kind"] == "reference"
+    # the same config object as the GPU arm prints for these arguments
+    import argparse
+    import bench
+    a = argparse.Namespace(side=200, steps=2, warmup=3)
+    assert d["config"] == bench.config_of(a, 2)
