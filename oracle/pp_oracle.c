@@ -50,6 +50,19 @@
 #include <stdlib.h>
 #include <string.h>
 
+/* Built with PPO_OMP (and -fopenmp), the loops over independent agents,
+ * cells and grid entries run on threads. Every draw is keyed by cell,
+ * iteration and rank, the per-cell actions touch only their cell, and the
+ * sums are of integers, so the results are identical to the single-threaded
+ * build; only the long full-size fixture runs use it. */
+#ifdef PPO_OMP
+#define PPO_FOR _Pragma("omp parallel for schedule(static)")
+#define PPO_FOR_DYN _Pragma("omp parallel for schedule(dynamic, 1024)")
+#else
+#define PPO_FOR
+#define PPO_FOR_DYN
+#endif
+
 /* Philox4x32-10, Salmon, Moraes, Dror, Shaw, "Parallel Random Numbers: As
  * Easy as 1, 2, 3", SC'11: round multipliers and Weyl key increments as
  * published there. */
@@ -141,6 +154,7 @@ ppo_state *ppo_create(const ppo_params *p, uint64_t seed, uint32_t capacity)
 		return NULL;
 	}
 	/* Grass: alive (0) w.p. 1/2, else 1 + U[0, restart) (pp_gpu.cl:383-393). */
+	PPO_FOR
 	for (uint32_t c = 0; c < C; c++) {
 		uint32_t r[4];
 		draw4(seed, c, 0, PPO_STREAM_INIT_CELL, 0, r);
@@ -151,6 +165,7 @@ ppo_state *ppo_create(const ppo_params *p, uint64_t seed, uint32_t capacity)
 	/* Agents: sheep first, then wolves (pp_gpu.cl:415-435); each cell's
 	 * list holds its agents in this creation order, i.e. the array is
 	 * stably sorted by cell. */
+	PPO_FOR
 	for (uint32_t a = 0; a < n0; a++) {
 		uint32_t r[4];
 		draw4(seed, a, 0, PPO_STREAM_INIT_AGENT, 0, r);
@@ -178,21 +193,35 @@ void ppo_destroy(ppo_state *s)
 
 static void agent_stats(uint32_t n, const uint32_t *en, ppo_stats *st)
 {
+	uint32_t sheep = 0, wolves = 0;
+	uint64_t sen = 0, wen = 0;
+#ifdef PPO_OMP
+	_Pragma("omp parallel for schedule(static) reduction(+:sheep, wolves, sen, wen)")
+#endif
 	for (uint32_t i = 0; i < n; i++) {
 		uint32_t e = energy_of(en[i]);
-		if (type_of(en[i])) { st->wolves++; st->wolves_en += e; }
-		else { st->sheep++; st->sheep_en += e; }
+		if (type_of(en[i])) { wolves++; wen += e; }
+		else { sheep++; sen += e; }
 	}
+	st->sheep += sheep; st->wolves += wolves;
+	st->sheep_en += sen; st->wolves_en += wen;
 }
 
 void ppo_stats_now(const ppo_state *s, ppo_stats *out)
 {
 	memset(out, 0, sizeof(*out));
 	agent_stats(s->n, s->en, out);
+	uint32_t alive = 0;
+	uint64_t sum = 0;
+#ifdef PPO_OMP
+	_Pragma("omp parallel for schedule(static) reduction(+:alive, sum)")
+#endif
 	for (uint32_t c = 0; c < s->p.grid_xy; c++) {
-		out->grass += s->grass[c] == 0;
-		out->grass_en += s->grass[c];
+		alive += s->grass[c] == 0;
+		sum += s->grass[c];
 	}
+	out->grass = alive;
+	out->grass_en = sum;
 }
 
 void ppo_move(const ppo_params *p, uint64_t seed, uint32_t iter, uint32_t n,
@@ -203,11 +232,25 @@ void ppo_move(const ppo_params *p, uint64_t seed, uint32_t iter, uint32_t n,
 	uint32_t emask = ppo_energy_mask(p);
 	/* rank[c] = agents of cell c seen so far: an agent's rank is its
 	 * position in its cell's list (earlier array entries of that cell). */
-	uint32_t *rank = calloc((size_t) C + 1, sizeof(uint32_t));
+	uint32_t *ks = malloc(sizeof(uint32_t) * (n ? n : 1));
+	uint32_t sorted = 1;
+	for (uint32_t i = 1; i < n && sorted; i++) sorted = cell_in[i - 1] <= cell_in[i];
+	if (sorted) {
+		/* a cell-sorted array (the simulation's state): the rank is the
+		 * distance to the cell's first entry */
+		for (uint32_t i = 0; i < n; i++)
+			ks[i] = (i > 0 && cell_in[i] == cell_in[i - 1]) ? ks[i - 1] + 1 : 0;
+	} else {
+		uint32_t *rank = calloc((size_t) C + 1, sizeof(uint32_t));
+		for (uint32_t i = 0; i < n; i++)
+			ks[i] = cell_in[i] < C ? rank[cell_in[i]]++ : 0;
+		free(rank);
+	}
+	PPO_FOR
 	for (uint32_t i = 0; i < n; i++) {
 		uint32_t en = en_in[i];
 		uint32_t e = energy_of(en);
-		uint32_t k = cell_in[i] < C ? rank[cell_in[i]]++ : 0;
+		uint32_t k = ks[i];
 		uint32_t e1 = (e - 1) & emask;
 		if (e1 == 0) {
 			cell_out[i] = C;           /* dead: sorts after every cell */
@@ -228,25 +271,42 @@ void ppo_move(const ppo_params *p, uint64_t seed, uint32_t iter, uint32_t n,
 		cell_out[i] = y * GX + x;
 		en_out[i] = (en & PPO_TYPE_BIT) | e1;
 	}
-	free(rank);
+	free(ks);
 }
 
 void ppo_sort(uint32_t n, const uint32_t *k_in, const uint32_t *v_in,
 	uint32_t *k_out, uint32_t *v_out, uint32_t max_key)
 {
-	uint32_t *cnt = calloc((size_t) max_key + 2, sizeof(uint32_t));
-	for (uint32_t i = 0; i < n; i++) cnt[k_in[i] + 1]++;
-	for (uint32_t k = 0; k <= max_key; k++) cnt[k + 1] += cnt[k];
-	for (uint32_t i = 0; i < n; i++) {
-		uint32_t pos = cnt[k_in[i]]++;
-		k_out[pos] = k_in[i];
-		v_out[pos] = v_in[i];
+	/* stable LSD radix sort on 16-bit digits (one pass for keys below 2^16,
+	 * two above) */
+	const uint32_t passes = max_key >> 16 ? 2 : 1;
+	uint32_t *cnt = malloc(sizeof(uint32_t) * 65537);
+	uint32_t *tk = passes > 1 ? malloc(sizeof(uint32_t) * (n ? n : 1)) : NULL;
+	uint32_t *tv = passes > 1 ? malloc(sizeof(uint32_t) * (n ? n : 1)) : NULL;
+	const uint32_t *ki = k_in, *vi = v_in;
+	for (uint32_t pass = 0; pass < passes; pass++) {
+		const uint32_t sh = 16 * pass;
+		uint32_t *ko = pass + 1 == passes ? k_out : tk;
+		uint32_t *vo = pass + 1 == passes ? v_out : tv;
+		memset(cnt, 0, sizeof(uint32_t) * 65537);
+		for (uint32_t i = 0; i < n; i++) cnt[((ki[i] >> sh) & 0xffffu) + 1]++;
+		for (uint32_t d = 0; d < 65536; d++) cnt[d + 1] += cnt[d];
+		for (uint32_t i = 0; i < n; i++) {
+			uint32_t pos = cnt[(ki[i] >> sh) & 0xffffu]++;
+			ko[pos] = ki[i];
+			vo[pos] = vi[i];
+		}
+		ki = ko;
+		vi = vo;
 	}
 	free(cnt);
+	free(tk);
+	free(tv);
 }
 
 void ppo_grass(uint32_t n_cells, uint16_t *grass)
 {
+	PPO_FOR
 	for (uint32_t c = 0; c < n_cells; c++)
 		if (grass[c] > 0) grass[c]--;
 }
@@ -333,10 +393,17 @@ int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
 	uint64_t out = 0;
 	int64_t ret;
 
-	uint32_t lo = 0;
-	while (lo < n) {
-		uint32_t c = cell[lo], hi = lo;
-		while (hi < n && cell[hi] == c) hi++;
+	/* the cells' segments of the cell-sorted array */
+	uint32_t nseg = 0;
+	for (uint32_t i = 0; i < n; i++) nseg += i == 0 || cell[i] != cell[i - 1];
+	uint32_t *seg = malloc(sizeof(uint32_t) * ((size_t) nseg + 1));
+	nseg = 0;
+	for (uint32_t i = 0; i < n; i++)
+		if (i == 0 || cell[i] != cell[i - 1]) seg[nseg++] = i;
+	seg[nseg] = n;
+	PPO_FOR_DYN
+	for (uint32_t q = 0; q < nseg; q++) {
+		uint32_t lo = seg[q], hi = seg[q + 1], c = cell[lo];
 		uint32_t m = hi - lo;
 		for (uint32_t j = 0; j < m; j++) {
 			uint32_t r[4];
@@ -348,8 +415,8 @@ int64_t ppo_act(const ppo_params *p, uint64_t seed, uint32_t iter,
 		ppo_act_cell(p, m, en + lo, prio + lo, dice + lo, &g, fin + lo,
 			kid + lo, haskid + lo, eaten + lo);
 		grass[c] = (uint16_t) g;
-		lo = hi;
 	}
+	free(seg);
 	for (uint32_t s = 0; s < n; s++) {
 		uint32_t tb = en[s] & PPO_TYPE_BIT;
 		if (!eaten[s]) {

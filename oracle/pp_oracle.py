@@ -38,6 +38,17 @@ class OStats(C.Structure):
 _lib = None
 
 
+def use_threads():
+    """Load the oracle built with its independent loops on OpenMP threads
+    (identical results; for generating long fixtures). Call before any
+    other use of this module."""
+    global _lib, LIB_PATH
+    if _lib is not None:
+        raise RuntimeError("oracle library already loaded")
+    from pphpc_gb300 import build as _b
+    LIB_PATH = _b.build_oracle(omp=True)
+
+
 def lib():
     global _lib
     if _lib is None:

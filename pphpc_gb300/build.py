@@ -99,13 +99,21 @@ def build_library(verbose=False, extra_nvflags=()):
     return LIB
 
 
-def build_oracle():
-    os.makedirs(os.path.dirname(ORACLE_LIB), exist_ok=True)
+ORACLE_LIB_OMP = os.path.join(ROOT, "oracle", "_build", "libpp_oracle_omp.so")
+
+
+def build_oracle(omp=False):
+    """The oracle (test infrastructure); with omp, the same source with its
+    independent loops on OpenMP threads (identical results), used only to
+    generate the long full-size fixtures."""
+    lib = ORACLE_LIB_OMP if omp else ORACLE_LIB
+    os.makedirs(os.path.dirname(lib), exist_ok=True)
     hdr = os.path.join(ROOT, "oracle", "pp_oracle.h")
-    if _newer(ORACLE_LIB, [ORACLE_SRC, hdr]):
-        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-Wall",
-              "-o", ORACLE_LIB, ORACLE_SRC])
-    return ORACLE_LIB
+    if _newer(lib, [ORACLE_SRC, hdr]):
+        extra = ["-fopenmp", "-DPPO_OMP"] if omp else []
+        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-Wall"] + extra +
+             ["-o", lib, ORACLE_SRC])
+    return lib
 
 
 def build_all(verbose=False):

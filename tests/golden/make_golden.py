@@ -98,6 +98,10 @@ def state_digest(cell, en, grass):
 
 
 def make_full_12800(name="12800v1_s2_full", every=250):
+    """Rows of the full-length 12800x12800 run, saved every `every`
+    iterations. With `--threads` the oracle built with its independent
+    loops on OpenMP threads runs it (identical results, several times
+    faster; pp_oracle.use_threads)."""
     d, seed, _, pool = LARGE["12800v1_s2_r300"]
     iters = d["iters"]
     st = orc.State(d, seed, capacity=pool)
@@ -165,7 +169,14 @@ def main():
 
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "large":
-        for n in sys.argv[2:] or sorted(LARGE) + ["12800v1_s2_full"]:
-            make_large(n)
+        names = [a for a in sys.argv[2:] if not a.startswith("--")]
+        if "--threads" in sys.argv:
+            orc.use_threads()
+        out = [a.split("=", 1)[1] for a in sys.argv[2:] if a.startswith("--out=")]
+        for n in names or sorted(LARGE) + ["12800v1_s2_full"]:
+            if n == "12800v1_s2_full" and out:
+                make_full_12800(out[0])
+            else:
+                make_large(n)
     else:
         main()
