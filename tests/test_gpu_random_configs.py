@@ -1,0 +1,66 @@
+"""Randomised configurations against the oracle, bit for bit: non-square
+grids, parameter values away from v1/v2 (thresholds of 0, probabilities of 0
+and 100, large gains), both iteration pipelines, several tile sizes and the
+three energy-field widths. Draws whose population outgrows the agent pool
+must make the library refuse the run as the oracle does. Each case is drawn
+from a fixed seed, so a failure names a case that can be rerun alone."""
+import numpy as np
+import pytest
+
+import pphpc_gb300 as pp
+from oracle import pp_oracle as orc
+from common import rows_array, first_diff
+
+pytestmark = pytest.mark.gpu
+
+N_CASES = 40
+
+
+def _case(k):
+    rng = np.random.default_rng(1000 + k)
+    gx = int(rng.choice([3, 7, 16, 50, 97, 128, 200, 333, 400]))
+    gy = int(rng.choice([3, 5, 16, 61, 100, 128, 257, 400]))
+    area = gx * gy
+    dens = float(rng.uniform(0.02, 0.3))
+    p = dict(init_sheep=int(area * dens * rng.uniform(0.3, 1.0)) + int(rng.integers(0, 3)),
+             init_wolves=int(area * dens * rng.uniform(0.1, 0.6)) + int(rng.integers(0, 3)),
+             sheep_gain_from_food=int(rng.choice([1, 4, 30, 200])),
+             sheep_reproduce_threshold=int(rng.integers(0, 7)),
+             sheep_reproduce_prob=int(rng.choice([0, 4, 10, 50, 100])),
+             wolves_gain_from_food=int(rng.choice([1, 10, 20, 300])),
+             wolves_reproduce_threshold=int(rng.integers(0, 7)),
+             wolves_reproduce_prob=int(rng.choice([0, 5, 20, 100])),
+             grass_restart=int(rng.integers(1, 21)),
+             grid_x=gx, grid_y=gy, iters=int(rng.integers(40, 301)))
+    sort_pipeline = bool(rng.random() < 0.35)
+    tile = int(rng.choice([0, 1024, 2048] if sort_pipeline else [0, 512, 1024, 2048, 4096]))
+    agent_size = int(rng.choice([0, 64, 32] if max(gx, gy) <= 1024 else [0, 64]))
+    seed = int(rng.integers(0, 1 << 40))
+    return p, seed, sort_pipeline, tile, agent_size
+
+
+@pytest.mark.parametrize("k", range(N_CASES))
+def test_random_config_matches_oracle(k):
+    d, seed, sort_pipeline, tile, agent_size = _case(k)
+    p = pp.make_params(**d)
+    bits = {0: 0, 64: 16, 32: 11}[agent_size]
+    n0 = p.init_sheep + p.init_wolves
+    pool = max(64 * n0, 8 * p.grid_x * p.grid_y) + 1024
+    kw = dict(max_agents=pool, sort_pipeline=sort_pipeline, tile_cells=tile,
+              agent_size=agent_size)
+    st = orc.State(p, seed, capacity=pool, energy_bits=bits)
+    try:
+        want = np.array([st.stats()] + [st.step() for _ in range(p.iters)], np.uint64)
+    except RuntimeError:
+        # the population outgrows the pool in the oracle: the library must
+        # refuse the run the same way (pp_gpu.c:847-852)
+        want = None
+    finally:
+        st.close()
+    if want is None:
+        with pytest.raises(pp.PPError) as e:
+            pp.run(p, seed, **kw)
+        assert e.value.code == pp.PP_OUT_OF_RESOURCES
+        return
+    got = rows_array(pp.run(p, seed, **kw))
+    assert first_diff(got, want) is None, (d, seed, sort_pipeline, tile, agent_size)
