@@ -277,31 +277,17 @@ void ppo_move(const ppo_params *p, uint64_t seed, uint32_t iter, uint32_t n,
 void ppo_sort(uint32_t n, const uint32_t *k_in, const uint32_t *v_in,
 	uint32_t *k_out, uint32_t *v_out, uint32_t max_key)
 {
-	/* stable LSD radix sort on 16-bit digits (one pass for keys below 2^16,
-	 * two above) */
-	const uint32_t passes = max_key >> 16 ? 2 : 1;
-	uint32_t *cnt = malloc(sizeof(uint32_t) * 65537);
-	uint32_t *tk = passes > 1 ? malloc(sizeof(uint32_t) * (n ? n : 1)) : NULL;
-	uint32_t *tv = passes > 1 ? malloc(sizeof(uint32_t) * (n ? n : 1)) : NULL;
-	const uint32_t *ki = k_in, *vi = v_in;
-	for (uint32_t pass = 0; pass < passes; pass++) {
-		const uint32_t sh = 16 * pass;
-		uint32_t *ko = pass + 1 == passes ? k_out : tk;
-		uint32_t *vo = pass + 1 == passes ? v_out : tv;
-		memset(cnt, 0, sizeof(uint32_t) * 65537);
-		for (uint32_t i = 0; i < n; i++) cnt[((ki[i] >> sh) & 0xffffu) + 1]++;
-		for (uint32_t d = 0; d < 65536; d++) cnt[d + 1] += cnt[d];
-		for (uint32_t i = 0; i < n; i++) {
-			uint32_t pos = cnt[(ki[i] >> sh) & 0xffffu]++;
-			ko[pos] = ki[i];
-			vo[pos] = vi[i];
-		}
-		ki = ko;
-		vi = vo;
+	/* stable counting sort: the moved agents are nearly in key order, so
+	 * its scatter runs nearly sequentially */
+	uint32_t *cnt = calloc((size_t) max_key + 2, sizeof(uint32_t));
+	for (uint32_t i = 0; i < n; i++) cnt[k_in[i] + 1]++;
+	for (uint32_t k = 0; k <= max_key; k++) cnt[k + 1] += cnt[k];
+	for (uint32_t i = 0; i < n; i++) {
+		uint32_t pos = cnt[k_in[i]]++;
+		k_out[pos] = k_in[i];
+		v_out[pos] = v_in[i];
 	}
 	free(cnt);
-	free(tk);
-	free(tv);
 }
 
 void ppo_grass(uint32_t n_cells, uint16_t *grass)
