@@ -144,7 +144,9 @@ __device__ __forceinline__ uint32_t step_excl_scan(uint32_t v, uint32_t *total)
  *         inbox of parity t) and the move of iteration t + 1 of its
  *         survivors and newborns into the group buffer of parity t + 1.
  *   !ACT: the move of iteration 1 of a freshly initialised run's agents,
- *         read cell-sorted from kS/vS at the tile offsets.
+ *         read from w.bucket at the tile offsets, where they lie in no
+ *         particular order with their creation indices (a cell's list is
+ *         its agents in creation order).
  * Phases (ACT): gather; counting sort by cell, each agent of a multi-agent
  * cell placed by its rank in canonical order; B draws; C actions, one
  * thread per agent (as the sort pipeline's act); E0 output offsets and
@@ -152,9 +154,8 @@ __device__ __forceinline__ uint32_t step_excl_scan(uint32_t v, uint32_t *total)
  * one warp allocates the tile's groups and posts them to the destination
  * tiles' inboxes; E2 records into the groups; per-tile stats. */
 template <int CPT, int NT, bool ACT>
-__device__ __forceinline__ void step_tile(const WorldDev &w,
-	const uint32_t *__restrict__ kS, const uint32_t *__restrict__ vS,
-	uint32_t tile, uint32_t out_base, uint32_t *sm)
+__device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
+	uint32_t out_base, uint32_t *sm)
 {
 	uint32_t *sk = sm, *sv = sm + w.act_cap, *sp = sv + w.act_cap,
 		*sd = sp + w.act_cap, *sperm = sd + w.act_cap;
@@ -216,7 +217,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 	 * k CPT + 4 a .. + 3 are the 16 bytes at word 4 (a NT + k), so a warp
 	 * reads its threads' counters with conflict-free 16-byte loads */
 #define SLOT(c) (((((c) % CPT) >> 2) * NT + (c) / CPT) * 4 + ((c) & 3))
-	if (ACT) {
+	{
 		uint4 *z = reinterpret_cast<uint4 *>(scnt);
 #pragma unroll
 		for (int q = 0; q < CPT / 4; q++) z[q * NT + tid] = make_uint4(0u, 0u, 0u, 0u);
@@ -273,11 +274,14 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 
 		uint32_t eats = 0;
 		if (!ACT) {
+			/* the tile's agents, counted per cell */
 			for (uint32_t j = tid; j < m; j += NT) {
-				LK[j] = kS[a0 + j] - c0;
-				LV[j] = vS[a0 + j];
+				const uint4 r = w.bucket[a0 + j];
+				const uint32_t kk = r.x - c0;
+				UK[j] = kk;
+				UV[j] = r.y;
+				atomicAdd(&scnt[SLOT(kk)], 1u);
 			}
-			__syncthreads();
 		} else {
 			/* gather the tile's groups and count agents per cell: item j comes
 			 * from the last group whose prefix is <= j (groups with equal
@@ -342,45 +346,47 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 					}
 				}
 			}
-			__syncthreads();
-			if (tid == 0) w.inbox_n[(size_t) pin * w.n_tiles + tile] = 0;
-			{
-				uint4 *s4 = reinterpret_cast<uint4 *>(scnt);
-				uint32_t loc = 0;
+		}
+		__syncthreads();
+		if (ACT && tid == 0) w.inbox_n[(size_t) pin * w.n_tiles + tile] = 0;
+		{
+			uint4 *s4 = reinterpret_cast<uint4 *>(scnt);
+			uint32_t loc = 0;
 #pragma unroll
-				for (int a = 0; a < CPT / 4; a++) {
-					const uint4 v = s4[a * NT + tid];
-					loc += v.x + v.y + v.z + v.w;
-				}
-				uint32_t tot;
-				uint32_t run_start = step_excl_scan<NT>(loc, &tot);
-#pragma unroll
-				for (int a = 0; a < CPT / 4; a++) {
-					const uint4 v = s4[a * NT + tid];
-					uint4 o;
-					o.x = run_start;
-					o.y = o.x + v.x;
-					o.z = o.y + v.y;
-					o.w = o.z + v.z;
-					run_start = o.w + v.w;
-					s4[a * NT + tid] = o;
-				}
+			for (int a = 0; a < CPT / 4; a++) {
+				const uint4 v = s4[a * NT + tid];
+				loc += v.x + v.y + v.z + v.w;
 			}
-			__syncthreads();
-			for (uint32_t j = tid; j < m; j += NT)
-				PERM[atomicAdd(&scnt[SLOT(UK[j] & lcmask)], 1u)] = j;
-			__syncthreads();
-			/* scnt[SLOT(c)] is now the end of cell c, and cell c's agents
-			 * occupy [end of c - 1, end of c) in arrival order; each goes to
-			 * the cell's start plus its rank in canonical order, which only
-			 * an agent sharing its cell has to count. LK holds the cell in
-			 * bits 0-15 and the rank in the cell's list in bits 16-31. */
-			for (uint32_t i = tid; i < m; i += NT) {
-				const uint32_t j = PERM[i];
-				const uint32_t rk = UK[j], c = rk & lcmask;
-				const uint32_t e = scnt[SLOT(c)], b = c ? scnt[SLOT(c - 1)] : 0;
-				uint32_t d = i;
-				if (e - b > 1) {
+			uint32_t tot;
+			uint32_t run_start = step_excl_scan<NT>(loc, &tot);
+#pragma unroll
+			for (int a = 0; a < CPT / 4; a++) {
+				const uint4 v = s4[a * NT + tid];
+				uint4 o;
+				o.x = run_start;
+				o.y = o.x + v.x;
+				o.z = o.y + v.y;
+				o.w = o.z + v.z;
+				run_start = o.w + v.w;
+				s4[a * NT + tid] = o;
+			}
+		}
+		__syncthreads();
+		for (uint32_t j = tid; j < m; j += NT)
+			PERM[atomicAdd(&scnt[SLOT(UK[j] & lcmask)], 1u)] = j;
+		__syncthreads();
+		/* scnt[SLOT(c)] is now the end of cell c, and cell c's agents
+		 * occupy [end of c - 1, end of c) in arrival order; each goes to
+		 * the cell's start plus its rank in canonical order, which only
+		 * an agent sharing its cell has to count. LK holds the cell in
+		 * bits 0-15 and the rank in the cell's list in bits 16-31. */
+		for (uint32_t i = tid; i < m; i += NT) {
+			const uint32_t j = PERM[i];
+			const uint32_t rk = UK[j], c = rk & lcmask;
+			const uint32_t e = scnt[SLOT(c)], b = c ? scnt[SLOT(c - 1)] : 0;
+			uint32_t d = i;
+			if (e - b > 1) {
+				if (ACT) {
 					const uint32_t lr = lt0 + c;
 					const uint32_t y = fastdiv_div(lr, run.gxdiv), x = lr - y * run.gx;
 					/* the cell's four neighbour offsets, then each mate's
@@ -401,13 +407,21 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 					d = b;
 					for (uint32_t q = b; q < e; q++)
 						d += okey(UK[PERM[q]]) < kx;
+				} else {
+					/* initial agents: creation order */
+					const uint32_t kx = w.bucket[a0 + j].z;
+					d = b;
+					for (uint32_t q = b; q < e; q++)
+						d += w.bucket[a0 + PERM[q]].z < kx;
 				}
-				if (d - b > 0xffffu) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
-				LK[d] = c | (d - b) << 16;
-				LV[d] = UV[j];
 			}
+			if (d - b > 0xffffu) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
+			LK[d] = c | (d - b) << 16;
+			LV[d] = UV[j];
+		}
 #undef SLOT
-			__syncthreads();
+		__syncthreads();
+		if (ACT) {
 			/* B: draws of every agent */
 			for (uint32_t j = tid; j < m; j += NT) {
 				const uint32_t lk = LK[j], lc = lk & 0xffffu;
@@ -436,7 +450,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 					w.grass[c0 + lc] = (uint16_t) (t16 + (uint16_t) ap.restart);
 					eats++;
 				}
-				LD[j] = kid;
+								LD[j] = kid;
 			}
 			__syncthreads();
 		}
@@ -509,10 +523,8 @@ __device__ __forceinline__ void step_tile(const WorldDev &w,
 				nb = 0;
 			}
 			const uint32_t lk = LK[j];
-			uint32_t f = j - (lk >> 16);
-			if (!ACT)
-				while (f > 0 && LK[f - 1] == lk) f--;
-			rank = o - (ACT ? LP[f] : f);
+			const uint32_t f = j - (lk >> 16);
+			rank = ACT ? o - LP[f] : lk >> 16;
 			en = nb ? (LD[j] & KID_ENERGY) : (LV[j] & ENERGY_MASK);
 		};
 
@@ -693,27 +705,25 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM(NT)) k_step_act(WorldDev w)
 {
 	extern __shared__ __align__(16) uint32_t sm[];
 	if (blockIdx.x >= min(w.ctr->tile_hi, w.n_tiles)) return;
-	step_tile<CPT, NT, true>(w, nullptr, nullptr, blockIdx.x, 0, sm);
+	step_tile<CPT, NT, true>(w, blockIdx.x, 0, sm);
 }
 
 /* The first move of a freshly initialised run: one CTA per tile of
  * [tile0, tile0 + gridDim.x). */
 template <int CPT, int NT>
 __global__ void __launch_bounds__(NT, CTAS_PER_SM(NT)) k_step_first(WorldDev w,
-	const uint32_t *__restrict__ kS, const uint32_t *__restrict__ vS,
 	uint32_t tile0, uint32_t out_base)
 {
 	extern __shared__ __align__(16) uint32_t sm[];
-	step_tile<CPT, NT, false>(w, kS, vS, tile0 + blockIdx.x, out_base, sm);
+	step_tile<CPT, NT, false>(w, tile0 + blockIdx.x, out_base, sm);
 }
 
 template <int CPT, int NT, bool ACT>
-void launch_one(const WorldDev &w, uint32_t grid, size_t smem,
-	const uint32_t *k, const uint32_t *v, uint32_t first, uint32_t out_base,
-	cudaStream_t s)
+void launch_one(const WorldDev &w, uint32_t grid, size_t smem, uint32_t first,
+	uint32_t out_base, cudaStream_t s)
 {
 	if (ACT) k_step_act<CPT, NT><<<grid, NT, smem, s>>>(w);
-	else k_step_first<CPT, NT><<<grid, NT, smem, s>>>(w, k, v, first, out_base);
+	else k_step_first<CPT, NT><<<grid, NT, smem, s>>>(w, first, out_base);
 }
 
 /* Thread count of a world's tile CTAs (see NT_SPARSE / NT_DENSE). */
@@ -724,9 +734,8 @@ inline int step_threads(const WorldDev &w)
 }
 
 template <bool ACT>
-cudaError_t launch_step(const WorldDev &w, const LaunchCfg &lc,
-	const uint32_t *k, const uint32_t *v, uint32_t first, uint32_t count,
-	uint32_t out_base, cudaStream_t s)
+cudaError_t launch_step(const WorldDev &w, const LaunchCfg &lc, uint32_t first,
+	uint32_t count, uint32_t out_base, cudaStream_t s)
 {
 	const uint32_t T = 1u << w.log_tile;
 	const size_t smem = (size_t) w.act_cap * 5 * sizeof(uint32_t)
@@ -734,18 +743,18 @@ cudaError_t launch_step(const WorldDev &w, const LaunchCfg &lc,
 	const uint32_t grid = ACT ? (uint32_t) std::max(1, lc.act_tiles) : count;
 	if (step_threads(w) == NT_DENSE) {
 		switch (T / NT_DENSE) {
-		case 4: launch_one<4, NT_DENSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
-		case 8: launch_one<8, NT_DENSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
-		case 16: launch_one<16, NT_DENSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
-		default: launch_one<32, NT_DENSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
+		case 4: launch_one<4, NT_DENSE, ACT>(w, grid, smem, first, out_base, s); break;
+		case 8: launch_one<8, NT_DENSE, ACT>(w, grid, smem, first, out_base, s); break;
+		case 16: launch_one<16, NT_DENSE, ACT>(w, grid, smem, first, out_base, s); break;
+		default: launch_one<32, NT_DENSE, ACT>(w, grid, smem, first, out_base, s); break;
 		}
 	} else {
 		switch (T / NT_SPARSE) {
-		case 4: launch_one<4, NT_SPARSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
-		case 8: launch_one<8, NT_SPARSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
-		case 16: launch_one<16, NT_SPARSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
-		case 32: launch_one<32, NT_SPARSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
-		default: launch_one<64, NT_SPARSE, ACT>(w, grid, smem, k, v, first, out_base, s); break;
+		case 4: launch_one<4, NT_SPARSE, ACT>(w, grid, smem, first, out_base, s); break;
+		case 8: launch_one<8, NT_SPARSE, ACT>(w, grid, smem, first, out_base, s); break;
+		case 16: launch_one<16, NT_SPARSE, ACT>(w, grid, smem, first, out_base, s); break;
+		case 32: launch_one<32, NT_SPARSE, ACT>(w, grid, smem, first, out_base, s); break;
+		default: launch_one<64, NT_SPARSE, ACT>(w, grid, smem, first, out_base, s); break;
 		}
 	}
 	return cudaGetLastError();
@@ -769,7 +778,7 @@ cudaError_t enqueue_iteration_fused(const WorldDev &w, const LaunchCfg &lc,
 	/* marks (optional, 3 events): before the act, after it, after the
 	 * finish */
 	if (marks) cudaEventRecord(marks[0], s);
-	cudaError_t e = launch_step<true>(w, lc, nullptr, nullptr, 0, w.n_tiles, 0, s);
+	cudaError_t e = launch_step<true>(w, lc, 0, w.n_tiles, 0, s);
 	if (e != cudaSuccess) return e;
 	if (marks) cudaEventRecord(marks[1], s);
 	e = launch_finish_fused(w, lc, s);
@@ -778,11 +787,10 @@ cudaError_t enqueue_iteration_fused(const WorldDev &w, const LaunchCfg &lc,
 }
 
 cudaError_t enqueue_move_groups(const WorldDev &w, const LaunchCfg &lc,
-	const uint32_t *k, const uint32_t *v, uint32_t first, uint32_t count,
-	uint32_t out_base, cudaStream_t s)
+	uint32_t first, uint32_t count, uint32_t out_base, cudaStream_t s)
 {
 	if (count == 0) return cudaSuccess;
-	return launch_step<false>(w, lc, k, v, first, count, out_base, s);
+	return launch_step<false>(w, lc, first, count, out_base, s);
 }
 
 cudaError_t set_step_smem_limits(size_t bytes)

@@ -25,6 +25,7 @@
  * an array position. Every kernel reads its sizes from device memory, so an
  * iteration is a fixed launch sequence, captured once as a CUDA graph.
  */
+#include <algorithm>
 #include <type_traits>
 
 #include "pp_kernels.cuh"
@@ -680,34 +681,53 @@ __global__ void k_after_sort(WorldCounters *ctr, uint32_t *hist)
 /* ------------------------------------------------------------------ */
 
 /* Initial grass of a run: countdown c (0 = alive) stored as the regrowth
- * iteration c, and c counted in the run's regrowth histogram. */
-__global__ void k_init_grass(WorldDev w, RunDev run)
+ * iteration c, c counted in the run's regrowth histogram (shared-memory
+ * atomics, cheaper here than a ballot per value), and the live cells and
+ * the countdown sum added to the run's stats row. */
+__global__ void __launch_bounds__(ACT_THREADS) k_init_grass(WorldDev w, RunDev run,
+	PPStatistics *dst)
 {
 	__shared__ uint32_t sh[1024];
+	__shared__ uint64_t red[2][ACT_THREADS / 32];
 	const uint32_t fs = run.restart + 1;
 	const bool local = fs <= 1024;
+	const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 	if (local)
 		for (uint32_t q = threadIdx.x; q < fs; q += blockDim.x) sh[q] = 0;
 	__syncthreads();
 	const uint32_t span = run.n_tiles << w.log_tile;
+	uint32_t alive_n = 0;
+	uint64_t csum = 0;
 	for (uint32_t lc = blockIdx.x * blockDim.x + threadIdx.x; lc < span;
 		lc += gridDim.x * blockDim.x) {
-		uint16_t v = 0;
+		uint32_t v = 0;
 		if (lc < run.ncells) {
 			u4 r = rng(run.seed_lo, run.seed_hi, lc, 0, STREAM_INIT_CELL, 0);
 			uint32_t alive = draw(r.x, 2);
-			v = alive ? 0 : (uint16_t) (1 + draw(r.y, run.restart));
-			if (v) {
-				if (local) atomicAdd(&sh[v], 1u);
-				else atomicAdd(&w.fring[run.fbase + v], 1u);
-			}
+			v = alive ? 0 : 1 + draw(r.y, run.restart);
+			alive_n += v == 0;
+			csum += v;
 		}
-		w.grass[run.cbase + lc] = v;
+		w.grass[run.cbase + lc] = (uint16_t) v;
+		if (v) {
+			if (local) atomicAdd(&sh[v], 1u);
+			else atomicAdd(&w.fring[run.fbase + v], 1u);
+		}
+	}
+	const uint64_t a = warp_sum((uint64_t) alive_n), g = warp_sum(csum);
+	if (lane == 0) {
+		red[0][wid] = a;
+		red[1][wid] = g;
 	}
 	__syncthreads();
 	if (local)
 		for (uint32_t q = threadIdx.x; q < fs; q += blockDim.x)
 			if (sh[q]) atomicAdd(&w.fring[run.fbase + q], sh[q]);
+	if (threadIdx.x < 2) {
+		uint64_t sum = 0;
+		for (uint32_t q = 0; q < ACT_THREADS / 32; q++) sum += red[threadIdx.x][q];
+		stats_atomic_add(dst, threadIdx.x ? 5u : 2u, sum);
+	}
 }
 
 /* Every alive cell's regrowth iteration moved to the run's current
@@ -728,10 +748,15 @@ __global__ void k_grass_rebase(WorldDev w)
 	}
 }
 
-/* Initial agents of a run, in creation order, into k/v[base ..). */
-__global__ void k_init_agents(RunDev run, uint32_t *k, uint32_t *v,
-	uint32_t base, uint32_t n_sheep, uint32_t n_wolves)
+/* Initial agents of a run, in creation order, into k/v[base ..); their
+ * counts and energy sums added to the run's stats row. */
+__global__ void __launch_bounds__(ACT_THREADS) k_init_agents(RunDev run,
+	uint32_t *k, uint32_t *v, uint32_t base, uint32_t n_sheep, uint32_t n_wolves,
+	PPStatistics *dst)
 {
+	__shared__ uint64_t s_part[6];
+	StatAcc acc;
+	acc.zero();
 	const uint32_t n = n_sheep + n_wolves;
 	for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < n;
 		a += gridDim.x * blockDim.x) {
@@ -742,44 +767,114 @@ __global__ void k_init_agents(RunDev run, uint32_t *k, uint32_t *v,
 		uint32_t e = (1 + draw(r.z, 2 * gain)) & run.emask;
 		k[base + a] = run.cbase + y * run.gx + x;
 		v[base + a] = (wolf ? TYPE_BIT : 0u) | e;
-	}
-}
-
-/* Stats of a run's current state: its agents vals[0, n), its cells. */
-__global__ void __launch_bounds__(ACT_THREADS) k_stats_run(WorldDev w,
-	RunDev run, const uint32_t *vals, uint32_t n, PPStatistics *dst)
-{
-	__shared__ uint64_t s_part[6];
-	StatAcc acc;
-	acc.zero();
-	const uint32_t stride = gridDim.x * blockDim.x;
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-		uint32_t v = vals[i], en = v & ENERGY_MASK;
-		if (v & TYPE_BIT) { acc.wolves++; acc.wen += en; }
-		else { acc.sheep++; acc.sen += en; }
-	}
-	/* the run's cells start on a tile boundary (16-byte aligned): eight
-	 * countdowns per 16-byte load, then the tail */
-	const uint4 *g8 = reinterpret_cast<const uint4 *>(w.grass + run.cbase);
-	const uint32_t n8 = run.ncells / 8;
-	for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n8; q += stride) {
-		const uint4 v = g8[q];
-		const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-		for (int k = 0; k < 4; k++) {
-			const uint32_t lo = wv[k] & 0xffffu, hi = wv[k] >> 16;
-			acc.galive += (lo == 0) + (hi == 0);
-			acc.gen += lo + hi;
-		}
-	}
-	for (uint32_t lc = n8 * 8 + blockIdx.x * blockDim.x + threadIdx.x;
-		lc < run.ncells; lc += stride) {
-		uint32_t gq = w.grass[run.cbase + lc];
-		acc.galive += gq == 0;
-		acc.gen += gq;
+		if (wolf) { acc.wolves++; acc.wen += e; }
+		else { acc.sheep++; acc.sen += e; }
 	}
 	block_stats(acc, s_part);
 	if (threadIdx.x < 6) stats_atomic_add(dst, threadIdx.x, s_part[threadIdx.x]);
+}
+
+/* Initial agents bucketed by tile (fused pipeline): agents per tile, the
+ * tiles' exclusive offsets, then each agent written into its tile's bucket
+ * as one 16-byte record with its creation index. A bucket's order is that
+ * of the atomics; the first move restores each cell's creation order from
+ * the indices. */
+__global__ void k_bucket_count(const uint32_t *k, uint32_t n, uint32_t log_tile,
+	uint32_t *cnt)
+{
+	for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < n;
+		a += gridDim.x * blockDim.x)
+		atomicAdd(&cnt[k[a] >> log_tile], 1u);
+}
+
+/* Exclusive scan in place of off[first, first + count] (the last entry
+ * enters as 0 and leaves as the total), copied to cursor[first, first +
+ * count), in chunks of BSCAN_CHUNK entries: the chunks' sums, then every
+ * chunk scanned from the sum of the chunks before it. */
+constexpr uint32_t BSCAN_THREADS = 1024, BSCAN_CHUNK = 4 * BSCAN_THREADS;
+
+__device__ __forceinline__ uint32_t bscan_block_excl(uint32_t x_in, uint32_t *ws,
+	uint32_t *total)
+{
+	const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	uint32_t x = x_in;
+#pragma unroll
+	for (int o = 1; o < 32; o <<= 1) {
+		const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+		if (lane >= (uint32_t) o) x += y;
+	}
+	if (lane == 31) ws[wid] = x;
+	__syncthreads();
+	if (wid == 0) {
+		uint32_t y = ws[lane];
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1) {
+			const uint32_t z = __shfl_up_sync(0xffffffffu, y, o);
+			if (lane >= (uint32_t) o) y += z;
+		}
+		ws[lane] = y;
+	}
+	__syncthreads();
+	*total = ws[BSCAN_THREADS / 32 - 1];
+	return (wid ? ws[wid - 1] : 0u) + x - x_in;
+}
+
+__global__ void __launch_bounds__(BSCAN_THREADS) k_bucket_sums(const uint32_t *off,
+	uint32_t first, uint32_t count, uint32_t *part)
+{
+	__shared__ uint32_t ws[BSCAN_THREADS / 32];
+	const uint32_t n = count + 1, c0 = blockIdx.x * BSCAN_CHUNK;
+	uint32_t sum = 0;
+#pragma unroll
+	for (int q = 0; q < 4; q++) {
+		const uint32_t i = c0 + q * BSCAN_THREADS + threadIdx.x;
+		if (i < n) sum += off[first + i];
+	}
+	uint32_t total;
+	bscan_block_excl(sum, ws, &total);
+	if (threadIdx.x == 0) part[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(BSCAN_THREADS) k_bucket_scan(uint32_t *off,
+	uint32_t *cursor, uint32_t first, uint32_t count, const uint32_t *part)
+{
+	__shared__ uint32_t ws[BSCAN_THREADS / 32];
+	const uint32_t n = count + 1, c0 = blockIdx.x * BSCAN_CHUNK;
+	/* the sum of the chunks before this one */
+	uint32_t before = 0;
+	for (uint32_t q = threadIdx.x; q < blockIdx.x; q += BSCAN_THREADS) before += part[q];
+	uint32_t total;
+	bscan_block_excl(before, ws, &total);
+	const uint32_t prefix = total;
+	__syncthreads();
+	uint32_t v[4], sum = 0;
+#pragma unroll
+	for (int q = 0; q < 4; q++) {
+		const uint32_t i = c0 + 4 * threadIdx.x + q;
+		v[q] = i < n ? off[first + i] : 0u;
+		sum += v[q];
+	}
+	uint32_t run = prefix + bscan_block_excl(sum, ws, &total);
+#pragma unroll
+	for (int q = 0; q < 4; q++) {
+		const uint32_t i = c0 + 4 * threadIdx.x + q;
+		if (i < n) {
+			off[first + i] = run;
+			if (i < count) cursor[first + i] = run;
+		}
+		run += v[q];
+	}
+}
+
+__global__ void k_bucket_scatter(const uint32_t *k, const uint32_t *v, uint32_t n,
+	uint32_t log_tile, uint32_t *cursor, uint4 *out)
+{
+	for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < n;
+		a += gridDim.x * blockDim.x) {
+		const uint32_t kk = k[a];
+		const uint32_t pos = atomicAdd(&cursor[kk >> log_tile], 1u);
+		out[pos] = make_uint4(kk, v[a], a, 0u);
+	}
 }
 
 /* Self-test of the bounded look-back the finish kernel uses: one warp per
@@ -886,35 +981,43 @@ cudaError_t enqueue_focal_init(const WorldDev &w, uint32_t r, uint32_t row,
 }
 
 cudaError_t enqueue_init_grass(const WorldDev &w, const RunDev &run,
-	cudaStream_t s)
+	uint32_t r, uint32_t row, cudaStream_t s)
 {
 	uint32_t span = run.n_tiles << w.log_tile;
-	uint32_t gb = (span + 255) / 256;
+	uint32_t gb = (span + ACT_THREADS - 1) / ACT_THREADS;
 	if (gb > 4096) gb = 4096;
 	if (gb == 0) gb = 1;
-	k_init_grass<<<gb, 256, 0, s>>>(w, run);
+	k_init_grass<<<gb, ACT_THREADS, 0, s>>>(w, run,
+		&w.ring[(size_t) row * w.nruns_cap + r]);
 	return cudaGetLastError();
 }
 
-cudaError_t enqueue_init_agents(const RunDev &run, uint32_t *k, uint32_t *v,
-	uint32_t base, uint32_t init_sheep, uint32_t init_wolves, cudaStream_t s)
+cudaError_t enqueue_init_agents(const WorldDev &w, const RunDev &run,
+	uint32_t r, uint32_t row, uint32_t *k, uint32_t *v, uint32_t base,
+	uint32_t init_sheep, uint32_t init_wolves, cudaStream_t s)
 {
 	uint32_t n = init_sheep + init_wolves;
 	if (!n) return cudaSuccess;
-	uint32_t ab = (n + 255) / 256;
+	uint32_t ab = (n + ACT_THREADS - 1) / ACT_THREADS;
 	if (ab > 4096) ab = 4096;
-	k_init_agents<<<ab, 256, 0, s>>>(run, k, v, base, init_sheep, init_wolves);
+	k_init_agents<<<ab, ACT_THREADS, 0, s>>>(run, k, v, base, init_sheep, init_wolves,
+		&w.ring[(size_t) row * w.nruns_cap + r]);
 	return cudaGetLastError();
 }
 
-cudaError_t enqueue_stats_run(const WorldDev &w, const RunDev &run,
-	uint32_t r, const uint32_t *vals, uint32_t n, uint32_t row, cudaStream_t s)
+cudaError_t enqueue_bucket_agents(const WorldDev &w, uint32_t n,
+	uint32_t first, uint32_t count, cudaStream_t s)
 {
-	uint32_t sb = (max(n, run.ncells / 8) + ACT_THREADS - 1) / ACT_THREADS;
-	if (sb > 2048) sb = 2048;
-	if (sb == 0) sb = 1;
-	k_stats_run<<<sb, ACT_THREADS, 0, s>>>(w, run, vals, n,
-		&w.ring[(size_t) row * w.nruns_cap + r]);
+	/* the fused pipeline does not use the region counters: they serve as
+	 * the buckets' fill cursors */
+	const uint32_t b = std::max<uint32_t>(1, std::min<uint32_t>((n + 255) / 256, 4096));
+	const uint32_t chunks = (count + 1 + BSCAN_CHUNK - 1) / BSCAN_CHUNK;
+	if (n) k_bucket_count<<<b, 256, 0, s>>>(w.kB, n, w.log_tile, w.tile_off);
+	k_bucket_sums<<<chunks, BSCAN_THREADS, 0, s>>>(w.tile_off, first, count, w.bscan);
+	k_bucket_scan<<<chunks, BSCAN_THREADS, 0, s>>>(w.tile_off, w.rcnt, first, count,
+		w.bscan);
+	if (n) k_bucket_scatter<<<b, 256, 0, s>>>(w.kB, w.vB, n, w.log_tile, w.rcnt,
+		w.bucket);
 	return cudaGetLastError();
 }
 

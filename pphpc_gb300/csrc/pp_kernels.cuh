@@ -9,12 +9,14 @@
 
 namespace pp {
 
-/* Everything one world iteration touches. The state between iterations is
- * the region buffer R: tile t's agents (its cells' lists, cell-sorted) at
- * [rstart[t], rstart[t] + rcnt[t]), with dense base dbase[t]. The move
- * reads the regions into the dense array B, the radix passes ping-pong
- * B <-> C, the act reads the sorted array and writes each tile's region
- * at twice its sorted offset. A (cap slots) is a dense copy for read-back. */
+/* Everything one world iteration touches. Sort pipeline: the state between
+ * iterations is the region buffer R: tile t's agents (its cells' lists,
+ * cell-sorted) at [rstart[t], rstart[t] + rcnt[t]), with dense base
+ * dbase[t]. The move reads the regions into the dense array B, the radix
+ * passes ping-pong B <-> C, the act reads the sorted array and writes each
+ * tile's region at twice its sorted offset. A (cap slots) is a dense copy
+ * for read-back. Both pipelines create agents into B. Arrays a pipeline
+ * does not use are not allocated (null). */
 struct WorldDev {
 	uint16_t *grass;          /* regrowth iteration per cell (see pp_device.cuh) */
 	uint32_t *fring;          /* per-run histograms of pending regrowth iterations */
@@ -47,6 +49,9 @@ struct WorldDev {
 	                           runs' first moves from 2 * cap on */
 	uint2 *inbox;             /* [2][n_tiles][IBX]                          */
 	uint32_t *inbox_n;        /* [2][n_tiles]                               */
+	uint4 *bucket;            /* [cap] initial agents bucketed by tile: cell,
+	                           type | energy, creation index (fused only)  */
+	uint32_t *bscan;          /* [n_tiles / 4096 + 2] bucket scan partials  */
 	FocalDev *focal;          /* [nruns_cap] running focal measures         */
 	uint32_t fused;
 };
@@ -74,11 +79,17 @@ cudaError_t enqueue_iteration_fused(const WorldDev &w, const LaunchCfg &lc,
 	cudaStream_t s, const cudaEvent_t *marks = nullptr);
 
 /* Fused pipeline: the first move of the agents of tiles [first, first +
- * count), cell-sorted in k/v (tile offsets in w.tile_off), into the group
- * buffer the next act reads. */
+ * count), bucketed by tile in w.bucket (tile offsets in w.tile_off), into
+ * the group buffer the next act reads. */
 cudaError_t enqueue_move_groups(const WorldDev &w, const LaunchCfg &lc,
-	const uint32_t *k, const uint32_t *v, uint32_t first, uint32_t count,
-	uint32_t out_base, cudaStream_t s);
+	uint32_t first, uint32_t count, uint32_t out_base, cudaStream_t s);
+
+/* Fused pipeline: the n agents in kB/vB (creation order) bucketed by tile
+ * into w.bucket with their creation indices; tile offsets of tiles [first,
+ * first + count] in w.tile_off (tile_off[first + count] = n), which must be
+ * zero on entry. */
+cudaError_t enqueue_bucket_agents(const WorldDev &w, uint32_t n,
+	uint32_t first, uint32_t count, cudaStream_t s);
 
 /* Fused pipeline: dense bases of the next act's per-tile inputs (after a
  * first move outside an iteration). */
@@ -97,15 +108,15 @@ cudaError_t launch_lookback_selftest(uint64_t *lb, uint32_t *ticket, uint32_t *e
 cudaError_t enqueue_focal_init(const WorldDev &w, uint32_t r, uint32_t row,
 	uint32_t t0, cudaStream_t s);
 
-/* Initialisation of a run: grass of its tiles; its initial agents in
- * creation order into k/v[base ..) (sorted by cell afterwards); the stats
- * of its agents A[base, base + n) and cells into ring row `row`. */
+/* Initialisation of run r: grass of its tiles; its initial agents in
+ * creation order into k/v[base ..) (bucketed or sorted by cell
+ * afterwards). Each adds its part of the run's stats (live cells and
+ * countdown sum; agent counts and energy sums) to ring row `row`. */
 cudaError_t enqueue_init_grass(const WorldDev &w, const RunDev &run,
-	cudaStream_t s);
-cudaError_t enqueue_init_agents(const RunDev &run, uint32_t *k, uint32_t *v,
-	uint32_t base, uint32_t init_sheep, uint32_t init_wolves, cudaStream_t s);
-cudaError_t enqueue_stats_run(const WorldDev &w, const RunDev &run,
-	uint32_t r, const uint32_t *vals, uint32_t n, uint32_t row, cudaStream_t s);
+	uint32_t r, uint32_t row, cudaStream_t s);
+cudaError_t enqueue_init_agents(const WorldDev &w, const RunDev &run,
+	uint32_t r, uint32_t row, uint32_t *k, uint32_t *v, uint32_t base,
+	uint32_t init_sheep, uint32_t init_wolves, cudaStream_t s);
 /* Regions of tiles [first, first + count) for a cell-sorted array of
  * ctr->aux_n agents at region-buffer offset `base`, then the dense bases
  * of all regions. */

@@ -63,10 +63,7 @@ World::~World() { free_all(); }
 void World::free_all()
 {
 	if (device_ >= 0 && !allocs_.empty()) cudaSetDevice(device_);
-	if (gexec_) cudaGraphExecDestroy(gexec_);
-	if (graph_) cudaGraphDestroy(graph_);
-	gexec_ = nullptr;
-	graph_ = nullptr;
+	drop_graph();
 	/* the buffers go back to the process cache only once no work of this
 	 * world can still touch them */
 	if (s_) cudaStreamSynchronize(s_);
@@ -216,15 +213,17 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 #define PP_AL(ptr, bytes) do { void *p_; rc = alloc((bytes), &p_); \
 	if (rc) return rc; (ptr) = (decltype(ptr)) p_; } while (0)
 	PP_AL(w_.grass, (size_t) w_.dead_key * sizeof(uint16_t));
-	PP_AL(w_.kA, cap * 4); PP_AL(w_.vA, cap * 4);
 	PP_AL(w_.kB, cap * 4); PP_AL(w_.vB, cap * 4);
-	PP_AL(w_.kC, cap * 4); PP_AL(w_.vC, cap * 4);
 	if (w_.fused) {
+		PP_AL(w_.bucket, cap * 16);
+		PP_AL(w_.bscan, ((size_t) tiles / 4096 + 2) * 4);
 		PP_AL(w_.kG0, 3 * cap * 4); PP_AL(w_.vG0, 3 * cap * 4);
 		PP_AL(w_.kG1, 3 * cap * 4); PP_AL(w_.vG1, 3 * cap * 4);
 		PP_AL(w_.inbox, (size_t) 2 * tiles * IBX * sizeof(uint2));
 		PP_AL(w_.inbox_n, (size_t) 2 * tiles * 4);
 	} else {
+		PP_AL(w_.kA, cap * 4); PP_AL(w_.vA, cap * 4);
+		PP_AL(w_.kC, cap * 4); PP_AL(w_.vC, cap * 4);
 		PP_AL(w_.kR, 3 * cap * 4); PP_AL(w_.vR, 3 * cap * 4);
 	}
 	PP_AL(w_.scratch_key, cap * 4); PP_AL(w_.scratch_val, cap * 4);
@@ -305,9 +304,10 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	lc_.act_tiles = (int) std::max<uint32_t>(tile_hi_, 1);
 
 	/* Initial state: grass, then every run's agents in creation order into
-	 * B at the run's base, sorted by cell into the region buffer (runs
-	 * occupy increasing cell ranges, so each run's agents stay at its
-	 * base), the tiles' regions and dense bases, stats row 0. */
+	 * B at the run's base; fused pipeline: bucketed by tile into A and
+	 * moved once; sort pipeline: sorted by cell into the region buffer, the
+	 * tiles' regions and dense bases (runs occupy increasing cell ranges,
+	 * so either way each run's agents stay at its base); stats row 0. */
 	std::vector<PPStatistics> resumed_row0(runs.size());
 	for (size_t r = 0; r < runs.size(); r++) {
 		if (runs[r].init_val) {
@@ -315,50 +315,40 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 			if (rc) return rc;
 			continue;
 		}
-		rc = cuda_status(enqueue_init_grass(w_, runs_h_[r], s_));
+		rc = cuda_status(enqueue_init_grass(w_, runs_h_[r], (uint32_t) r, 0, s_));
 		if (rc) return rc;
-		rc = cuda_status(enqueue_init_agents(runs_h_[r], w_.kB, w_.vB, base_h[r],
+		rc = cuda_status(enqueue_init_agents(w_, runs_h_[r], (uint32_t) r, 0,
+			w_.kB, w_.vB, base_h[r],
 			runs[r].p.init_sheep, runs[r].p.init_wolves, s_));
 		if (rc) return rc;
 	}
-	uint32_t *sorted_v;
 	if (w_.fused) {
-		/* sorted into A; the first move of every agent into the group
+		/* bucketed by tile; the first move of every agent into the group
 		 * buffer the first act reads */
-		rc = sort_into(base, w_.kA, w_.vA);
+		rc = place_bucketed(base, 0, (uint32_t) tiles, 0);
 		if (rc) return rc;
-		rc = place_sorted(base, 0, (uint32_t) tiles, 0);
-		if (rc) return rc;
-		sorted_v = w_.vA;
 	} else {
 		rc = sort_into(base, w_.kR, w_.vR);
 		if (rc) return rc;
 		rc = cuda_status(enqueue_regions_from_sorted(w_, lc_, w_.kR, 0, (uint32_t) tiles, 0, s_));
 		if (rc) return rc;
-		sorted_v = w_.vR;
 	}
+	/* row 0: summed by the init kernels, or the resumed state's */
 	for (size_t r = 0; r < runs.size(); r++) {
-		if (runs[r].init_val) {
-			PP_CK(cudaMemcpyAsync(&w_.ring[r], &resumed_row0[r], sizeof(PPStatistics),
-				cudaMemcpyHostToDevice, s_));
-			h2d_ += sizeof(PPStatistics);
-			continue;
-		}
-		rc = cuda_status(enqueue_stats_run(w_, runs_h_[r], (uint32_t) r,
-			sorted_v + base_h[r], runs[r].p.init_sheep + runs[r].p.init_wolves, 0, s_));
-		if (rc) return rc;
+		if (!runs[r].init_val) continue;
+		PP_CK(cudaMemcpyAsync(&w_.ring[r], &resumed_row0[r], sizeof(PPStatistics),
+			cudaMemcpyHostToDevice, s_));
+		h2d_ += sizeof(PPStatistics);
 	}
 	for (size_t r = 0; r < runs.size(); r++) {
 		rc = cuda_status(enqueue_focal_init(w_, (uint32_t) r, 0, runs[r].start_iter, s_));
 		if (rc) return rc;
 	}
 	giter_ = 0;
+	/* the graph of graph_iters iterations is captured by the first call
+	 * that runs that many in a row, so a short job never pays for it */
 	graph_iters_ = cfg.graph_iters;
 	PP_CK(cudaStreamSynchronize(s_));
-	if (graph_iters_) {
-		rc = build_graph();
-		if (rc) return rc;
-	}
 	return PP_SUCCESS;
 }
 
@@ -437,17 +427,18 @@ int World::sort_into(uint32_t n, uint32_t *dst_k, uint32_t *dst_v)
 	return PP_SUCCESS;
 }
 
-int World::place_sorted(uint32_t n, uint32_t first, uint32_t count,
+int World::place_bucketed(uint32_t n, uint32_t first, uint32_t count,
 	uint32_t out_base)
 {
-	/* tile offsets of the n cell-sorted agents in A (count from
-	 * ctr->aux_n), the first move of the agents of tiles [first, first +
-	 * count) into the group buffer from out_base on, then the dense input
-	 * bases of the next act */
-	(void) n;
-	PP_CK(launch_offsets(w_.kA, &w_.ctr->aux_n, w_.log_tile, w_.n_tiles,
-		w_.tile_off, lc_.offs_blocks, s_));
-	PP_CK(enqueue_move_groups(w_, lc_, w_.kA, w_.vA, first, count, out_base, s_));
+	/* the n agents of B (creation order, all in tiles [first, first +
+	 * count)) bucketed by tile with their creation indices (no sort:
+	 * the first move orders each cell's agents), fresh look-back epochs as
+	 * after a sort, the first move of those tiles' agents into the group
+	 * buffer from out_base on, then the dense input bases of the next act */
+	PP_CK(cudaMemsetAsync(w_.tile_off + first, 0, ((size_t) count + 1) * 4, s_));
+	PP_CK(enqueue_bucket_agents(w_, n, first, count, s_));
+	PP_CK(enqueue_after_sort(w_.ctr, w_.hist, s_));
+	PP_CK(enqueue_move_groups(w_, lc_, first, count, out_base, s_));
 	PP_CK(enqueue_fused_bases(w_, lc_, s_));
 	return PP_SUCCESS;
 }
@@ -458,10 +449,15 @@ cudaError_t World::enqueue_one(const cudaEvent_t *marks)
 		: enqueue_iteration(w_, lc_, s_, marks);
 }
 
-int World::build_graph()
+void World::drop_graph()
 {
 	if (gexec_) { cudaGraphExecDestroy(gexec_); gexec_ = nullptr; }
 	if (graph_) { cudaGraphDestroy(graph_); graph_ = nullptr; }
+}
+
+int World::build_graph()
+{
+	drop_graph();
 	PP_CK(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
 	for (uint32_t i = 0; i < graph_iters_; i++) {
 		cudaError_t e = enqueue_one();
@@ -477,6 +473,13 @@ int World::build_graph()
 	return PP_SUCCESS;
 }
 
+int World::prepare_graph(uint32_t n)
+{
+	PP_CK(cudaSetDevice(device_));
+	if (graph_iters_ && !gexec_ && n >= graph_iters_) return build_graph();
+	return PP_SUCCESS;
+}
+
 int World::enqueue(uint32_t n)
 {
 	PP_CK(cudaSetDevice(device_));
@@ -487,7 +490,11 @@ int World::enqueue(uint32_t n)
 		uint32_t to_rebase = REBASE - (giter_ % REBASE);
 		uint32_t stretch = std::min(n - done, to_rebase);
 		uint32_t k = 0;
-		if (gexec_ && graph_iters_) {
+		if (graph_iters_ && stretch >= graph_iters_) {
+			if (!gexec_) {
+				const int rc = build_graph();
+				if (rc) return rc;
+			}
 			while (stretch - k >= graph_iters_) {
 				PP_CK(cudaGraphLaunch(gexec_, s_));
 				k += graph_iters_;
@@ -767,8 +774,9 @@ int World::update_tile_hi()
 	PP_CK(cudaMemcpyAsync(&w_.ctr->tile_hi, &tile_hi_, 4, cudaMemcpyHostToDevice, s_));
 	PP_CK(cudaStreamSynchronize(s_));
 	h2d_ += 4;
-	/* the captured iterations carry the old grid */
-	if (gexec_ && graph_iters_) return build_graph();
+	/* the captured iterations carry the old grid: captured again when next
+	 * needed */
+	drop_graph();
 	return PP_SUCCESS;
 }
 
@@ -821,22 +829,19 @@ int World::admit(const RunSpec &spec, uint32_t *slot_out)
 	if (rc0) return rc0;
 	uint32_t row = giter_ % w_.ring_rows;
 	PP_CK(cudaMemsetAsync(&w_.ring[(size_t) row * w_.nruns_cap + slot], 0, sizeof(PPStatistics), s_));
-	/* Grass of its tiles; its agents sorted by cell and appended to A. The
-	 * other runs' agents stay in place: draws never depend on positions. */
-	int rc = cuda_status(enqueue_init_grass(w_, run, s_));
+	/* Grass of its tiles; its agents bucketed by tile (fused pipeline) or
+	 * sorted by cell (sort pipeline), and moved in. The other runs' agents
+	 * stay in place: draws never depend on positions. */
+	int rc = cuda_status(enqueue_init_grass(w_, run, slot, row, s_));
 	if (rc) return rc;
-	rc = cuda_status(enqueue_init_agents(run, w_.kB, w_.vB, 0,
+	rc = cuda_status(enqueue_init_agents(w_, run, slot, row, w_.kB, w_.vB, 0,
 		spec.p.init_sheep, spec.p.init_wolves, s_));
 	if (rc) return rc;
 	if (w_.fused) {
-		/* sorted into A, moved into the group buffer the next act reads */
-		rc = sort_into(n0, w_.kA, w_.vA);
-		if (rc) return rc;
-		rc = place_sorted(n0, first, need, 2 * w_.cap + adm_used_);
+		/* bucketed into A, moved into the group buffer the next act reads */
+		rc = place_bucketed(n0, first, need, 2 * w_.cap + adm_used_);
 		if (rc) return rc;
 		adm_used_ += n0;
-		rc = cuda_status(enqueue_stats_run(w_, run, slot, w_.vA, n0, row, s_));
-		if (rc) return rc;
 		PP_CK(cudaStreamSynchronize(s_));
 		rc = cuda_status(enqueue_focal_init(w_, slot, row, 0, s_));
 		if (rc) return rc;
@@ -850,8 +855,6 @@ int World::admit(const RunSpec &spec, uint32_t *slot_out)
 		rc = cuda_status(enqueue_regions_from_sorted(w_, lc_, w_.kR + adm, first, need, adm, s_));
 		if (rc) return rc;
 		adm_used_ += n0;
-		rc = cuda_status(enqueue_stats_run(w_, run, slot, w_.vR + adm, n0, row, s_));
-		if (rc) return rc;
 		rc = cuda_status(enqueue_focal_init(w_, slot, row, 0, s_));
 		if (rc) return rc;
 	}
@@ -1226,10 +1229,12 @@ extern "C" int pp_sim_time(pp_sim *sim, uint32_t n_iters, float *ms)
 	World &w = sim->world;
 	cudaEvent_t a, b;
 	PP_CK(cudaSetDevice(w.dev_index()));
+	int rc = w.prepare_graph(n_iters);
+	if (rc) return rc;
 	PP_CK(cudaEventCreate(&a));
 	PP_CK(cudaEventCreate(&b));
 	PP_CK(cudaEventRecord(a, w.stream()));
-	int rc = w.enqueue(n_iters);
+	rc = w.enqueue(n_iters);
 	PP_CK(cudaEventRecord(b, w.stream()));
 	if (rc == PP_SUCCESS) rc = w.sync_check();
 	if (rc == PP_SUCCESS) PP_CK(cudaEventElapsedTime(ms, a, b));

@@ -79,6 +79,9 @@ public:
 
 	/* Enqueue n iterations; no host synchronisation. */
 	int enqueue(uint32_t n);
+	/* capture the iteration graph now if a call of n iterations would, so
+	 * that a timed call does not include the capture */
+	int prepare_graph(uint32_t n);
 
 	/* Wait and check the device error flags. */
 	int sync_check();
@@ -125,11 +128,12 @@ private:
 	int load_run_state(const RunSpec &spec, const RunDev &run, uint32_t base,
 		PPStatistics *row0);
 	int build_graph();
+	void drop_graph();
 	int init_run_device(uint32_t r, uint32_t base, const RunSpec &spec);
 	cudaError_t enqueue_one(const cudaEvent_t *marks = nullptr);
 	int get_state_fused(uint32_t *cell, uint32_t *en, uint32_t n_max,
 		uint32_t *n_out, uint32_t r);
-	int place_sorted(uint32_t n, uint32_t first, uint32_t count,
+	int place_bucketed(uint32_t n, uint32_t first, uint32_t count,
 		uint32_t out_base);
 	void free_all();
 
