@@ -232,21 +232,22 @@ REF_MAX_AGENTS = 1 << 27   # the reference's -m for the 12800^2 workload (1 GiB 
 
 def workload(pp, args):
     """The plain workload: 12800 x 12800 v1 by default; --side scales the
-    grid (agents by area) for smaller cases of the same kernels."""
-    if args.side == 12800:
+    grid (agents by area) for smaller cases of the same kernels, --params
+    picks the parameter set."""
+    if args.side == 12800 and args.params == "v1":
         return pp.make_params(**WORKLOAD), WORKLOAD_NAME
-    p = scaled_params(pp, args.side, 1, WORKLOAD["iters"])
-    return p, "pphpc-%dx%d-v1" % (args.side, args.side)
+    p = scaled_params(pp, args.side, 1 if args.params == "v1" else 2, WORKLOAD["iters"])
+    return p, "pphpc-%dx%d-%s" % (args.side, args.side, args.params)
 
 
 def workload_dict(args):
     """The plain workload as a parameter dict (no library needed)."""
     wl, wname = dict(WORKLOAD), WORKLOAD_NAME
-    if args.side != 12800:
+    if args.side != 12800 or args.params != "v1":
         a = args.side * args.side
         wl.update(grid_x=args.side, grid_y=args.side, init_sheep=a * 4 // 100,
-                  init_wolves=a * 2 // 100)
-        wname = "pphpc-%dx%d-v1" % (args.side, args.side)
+                  init_wolves=a * 2 // 100, **(V1 if args.params == "v1" else V2))
+        wname = "pphpc-%dx%d-%s" % (args.side, args.side, args.params)
     return wl, wname
 
 
@@ -254,7 +255,7 @@ def config_of(args, world):
     """The `config` object, identical in both arms."""
     wl, wname = workload_dict(args)
     return {"workload": wname, "grid": "%dx%d" % (wl["grid_x"], wl["grid_y"]),
-            "params": "v1", "init_sheep": wl["init_sheep"],
+            "params": args.params, "init_sheep": wl["init_sheep"],
             "init_wolves": wl["init_wolves"], "seed": SEED,
             "timed_iterations": "%d..%d" % (args.warmup + 1, args.warmup + args.steps),
             "l2": "inputs larger than L2 (working set ~2 GB on the GPU)",
@@ -694,6 +695,8 @@ def main():
                     help="requests of the served stream (0 = skip the leg)")
     ap.add_argument("--side", type=int, default=12800,
                     help="grid side of the plain workload (agents scale by area)")
+    ap.add_argument("--params", choices=["v1", "v2"], default="v1",
+                    help="parameter set of the plain workload")
     ap.add_argument("--tile-cells", type=int, default=0,
                     help="cells per act tile (0 = the library's choice)")
     args = ap.parse_args()

@@ -259,7 +259,13 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 	}
 	__syncthreads();
 	if (!in_smem && s_fail) {
-		if (ACT) cp_async_wait_all();
+		/* the tile's agents are dropped (the overflow is flagged): its
+		 * inbox is emptied as if it had been read, so no later act reads
+		 * these groups again */
+		if (ACT) {
+			cp_async_wait_all();
+			if (tid == 0) w.inbox_n[(size_t) pin * w.n_tiles + tile] = 0;
+		}
 		if (tid < 8) w.part[(size_t) tile * 8 + tid] = 0;
 		return;
 	}
@@ -378,8 +384,11 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 		/* scnt[SLOT(c)] is now the end of cell c, and cell c's agents
 		 * occupy [end of c - 1, end of c) in arrival order; each goes to
 		 * the cell's start plus its rank in canonical order, which only
-		 * an agent sharing its cell has to count. LK holds the cell in
-		 * bits 0-15 and the rank in the cell's list in bits 16-31. */
+		 * an agent sharing its cell has to count. Equal keys, which a
+		 * consistent state never holds, are ordered by arrival, so the
+		 * slots stay a permutation whatever the input (after an overflow,
+		 * say). LK holds the cell in bits 0-15 and the rank in the cell's
+		 * list in bits 16-31. */
 		for (uint32_t i = tid; i < m; i += NT) {
 			const uint32_t j = PERM[i];
 			const uint32_t rk = UK[j], c = rk & lcmask;
@@ -405,14 +414,19 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 					};
 					const int64_t kx = okey(rk);
 					d = b;
-					for (uint32_t q = b; q < e; q++)
-						d += okey(UK[PERM[q]]) < kx;
+					for (uint32_t q = b; q < e; q++) {
+						const uint32_t jq = PERM[q];
+						const int64_t kq = okey(UK[jq]);
+						d += kq < kx || (kq == kx && jq < j);
+					}
 				} else {
 					/* initial agents: creation order */
 					const uint32_t kx = w.bucket[a0 + j].z;
 					d = b;
-					for (uint32_t q = b; q < e; q++)
-						d += w.bucket[a0 + PERM[q]].z < kx;
+					for (uint32_t q = b; q < e; q++) {
+						const uint32_t jq = PERM[q], kq = w.bucket[a0 + jq].z;
+						d += kq < kx || (kq == kx && jq < j);
+					}
 				}
 			}
 			if (d - b > 0xffffu) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
@@ -450,7 +464,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 					w.grass[c0 + lc] = (uint16_t) (t16 + (uint16_t) ap.restart);
 					eats++;
 				}
-								LD[j] = kid;
+				LD[j] = kid;
 			}
 			__syncthreads();
 		}

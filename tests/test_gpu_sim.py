@@ -85,6 +85,20 @@ def test_crowded_cells(sort_pipeline):
                max_agents=400_000, sort_pipeline=sort_pipeline)
 
 
+def test_pool_overflow_at_scale_is_refused():
+    """A pool far below the population: 3200^2 v2 grows to 27 times its
+    initial agents while the pool holds 5 times, and on 512-cell tiles most
+    tiles outgrow both their shared memory and the global scratch, for
+    hundreds of iterations. The run is refused with PP_OUT_OF_RESOURCES
+    (pp_gpu.c:847-852), and the device stays usable."""
+    p = params(3200, 2, iters=300)
+    n0 = p.init_sheep + p.init_wolves
+    with pytest.raises(pp.PPError) as ei:
+        pp.run(p, 2, max_agents=5 * n0, tile_cells=512)
+    assert ei.value.code == pp.PP_OUT_OF_RESOURCES
+    _check_run(params(40, 1), 3, 60)
+
+
 @PIPES
 def test_state_bit_exact_after_steps(sort_pipeline):
     p = params(40, 2)
