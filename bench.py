@@ -321,7 +321,9 @@ def run_ours(args, dist):
     dev = dist.local
     p, wname = workload(pp, args)
     n0 = p.init_sheep + p.init_wolves
-    cap = 5 * n0
+    # pool: 5x the initial agents for v1 (its population peaks at 4.25x),
+    # 40x for v2 (it peaks near 27x), as the batched and served pools
+    cap = (5 if args.params == "v1" else 40) * n0
     K, W = args.steps, args.warmup
 
     # -- launch geometry from the autotuner (or --tile-cells) --

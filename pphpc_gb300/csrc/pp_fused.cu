@@ -433,7 +433,6 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 			LK[d] = c | (d - b) << 16;
 			LV[d] = UV[j];
 		}
-#undef SLOT
 		__syncthreads();
 		if (ACT) {
 			/* B: draws of every agent */
@@ -455,9 +454,10 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 			const uint16_t t16 = (uint16_t) t;
 			for (uint32_t j = tid; j < m; j += NT) {
 				const uint32_t lk = LK[j], lc = lk & 0xffffu;
+				/* the cell's agents are [p, e): the counters hold each
+				 * cell's end since the copy into cell order */
 				const uint32_t p = j - (lk >> 16);
-				uint32_t e = j + 1;
-				while (e < m && (LK[e] >> 16) != 0) e++;
+				const uint32_t e = scnt[SLOT(lc)];
 				const int32_t dd = (int16_t) (uint16_t) (sgrass[lc] - t16);
 				uint32_t kid;
 				if (act_agent(j, p, e, LV, LP, ap, dd > 0 ? (uint32_t) dd : 0u, LD[j], &kid)) {
@@ -469,6 +469,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 			__syncthreads();
 		}
 
+#undef SLOT
 		/* ---- E0: output offsets (each survivor, then its newborn), stats,
 		 * and the output -> agent map OUTJ (agent index | newborn << 15) ---- */
 		const uint32_t ch = (m + NT - 1) / NT;

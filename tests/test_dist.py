@@ -73,5 +73,5 @@ def test_reference_arm_under_torchrun_prints_one_line():
     # the same config object as the GPU arm prints for these arguments
     import argparse
     import bench
-    a = argparse.Namespace(side=200, steps=2, warmup=3)
+    a = argparse.Namespace(side=200, params="v1", steps=2, warmup=3)
     assert d["config"] == bench.config_of(a, 2)
