@@ -122,7 +122,11 @@ typedef struct pp_opts {
 	uint32_t tile_cells;    /* cells per act tile: 1024..8192, or 512 for the
 	                           fused pipeline; 0 = choose (or autotune)    */
 	uint32_t sort_digit_bits; /* radix digit width 4..8; 0 = autotune         */
-	uint32_t use_graph;     /* capture each iteration as a CUDA graph (1) or not (0) */
+	uint32_t use_graph;     /* 1: run iterations as CUDA graphs of 32, captured
+	                           by the first call that runs 32 in a row (a
+	                           simulation created inside a stream capture
+	                           should make that call outside it); 0: launch
+	                           by launch */
 	uint32_t sort_pipeline; /* 1 = per-iteration sort pipeline (move, LSD radix
 	                           passes over the tile bits, tile offsets, act);
 	                           0 = fused act+move with a gather by destination
