@@ -323,7 +323,7 @@ def run_ours(args, dist):
     p, wname = workload(pp, args)
     n0 = p.init_sheep + p.init_wolves
     # pool: 5x the initial agents for v1 (its population peaks at 4.25x),
-    # 40x for v2 (it peaks near 27x), as the batched and served pools
+    # 40x for v2 (it peaks at 27x to 36x), as the batched and served pools
     cap = (5 if args.params == "v1" else 40) * n0
     K, W = args.steps, args.warmup
 

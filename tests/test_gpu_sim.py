@@ -86,8 +86,8 @@ def test_crowded_cells(sort_pipeline):
 
 
 def test_pool_overflow_at_scale_is_refused():
-    """A pool far below the population: 3200^2 v2 grows to 27 times its
-    initial agents while the pool holds 5 times, and on 512-cell tiles most
+    """A pool far below the population: 3200^2 v2 grows to about 27 times
+    its initial agents while the pool holds 5 times, and on 512-cell tiles most
     tiles outgrow both their shared memory and the global scratch, for
     hundreds of iterations. The run is refused with PP_OUT_OF_RESOURCES
     (pp_gpu.c:847-852), and the device stays usable."""
