@@ -50,6 +50,10 @@ constexpr uint32_t CLS_FOREIGN = 30;   /* classes 0..29: other destination tiles
 constexpr uint32_t CLS_OWN = 30;       /* moved within the tile                  */
 constexpr uint32_t CLS_GRAVE = 31;     /* dead and parked records                */
 constexpr uint32_t CLS_NONE = 0xffffffffu;   /* table full: record dropped (error) */
+/* direction code of a dropped output in the move phase's record cache (no
+ * record carries it: records use 0-4, DIR_PARKED and DIR_DEAD) */
+constexpr uint32_t DIR_DROPPED = 5;
+static_assert(DIR_DROPPED != DIR_PARKED && DIR_DROPPED != DIR_DEAD, "cache code");
 constexpr uint32_t TBL_EMPTY = 0xffffffffu;
 
 /* Class of destination tile dt (not the CTA's own tile) in the CTA's table
@@ -544,13 +548,14 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 		};
 
 		/* ---- E1: move draws of the outputs, per-class counts; with room in
-		 * the cell counters' words (2 act_cap <= T) and offsets that fit 10
-		 * bits (2 act_cap <= 1024), each output's cell in its destination
-		 * tile (bits 0-12), direction (13-15), class (16-21) and offset in its
-		 * class's group (22-31) are kept for E2, else only its direction ---- */
+		 * the cell counters' words (2 act_cap <= T) and offsets that fit 11
+		 * bits (2 act_cap <= 2048), each output's cell in its destination
+		 * tile (bits 0-12), direction (13-15; DIR_DROPPED for an output
+		 * counted nowhere), class (16-20) and offset in its class's group
+		 * (21-31) are kept for E2, else only its direction ---- */
 		bool bad = false;
 		const bool cache = in_smem && 2u * w.act_cap <= (uint32_t) (CPT * NT)
-			&& 2u * w.act_cap <= 1024u;
+			&& 2u * w.act_cap <= 2048u;
 		uint32_t *DEST = scnt;
 		for (uint32_t o = tid; o < total; o += NT) {
 			uint32_t j, nb, en, rank;
@@ -576,7 +581,9 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 				cls = NCLS;                      /* counted nowhere */
 			}
 			const uint32_t off = warp_agg_add(s_ccnt, cls);
-			if (cache) DEST[o] = klo | (code << REC_DIR_SHIFT) | (cls << 16) | (off << 22);
+			if (cache)
+				DEST[o] = cls == NCLS ? DIR_DROPPED << REC_DIR_SHIFT
+					: klo | (code << REC_DIR_SHIFT) | (cls << 16) | (off << 21);
 			else DIR[o] = (uint8_t) code;
 		}
 		if (bad) atomicOr(&w.ctr->err, ERRF_OVERFLOW);
@@ -625,11 +632,11 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 				if (cache) {
 					const uint32_t d = DEST[o];
 					const uint32_t code = (d >> REC_DIR_SHIFT) & 7u;
-					cls = (d >> 16) & 63u;
+					cls = (d >> 16) & 31u;
 					key = (d & 0xffffu) | (rank << REC_RANK_SHIFT);
 					val = code >= DIR_PARKED ? (tb | en) : (tb | ((en - 1) & run.emask));
-					const uint32_t pos = s_cpos[cls] + (d >> 22);
-					if (cls != NCLS) {
+					const uint32_t pos = s_cpos[cls] + (d >> 21);
+					if (code != DIR_DROPPED) {
 						kGo[pos] = key;
 						vGo[pos] = val;
 					}
@@ -742,10 +749,22 @@ void launch_one(const WorldDev &w, uint32_t grid, size_t smem, uint32_t first,
 }
 
 /* Thread count of a world's tile CTAs (see NT_SPARSE / NT_DENSE). */
+inline int step_threads_for(uint32_t T, uint32_t act_cap)
+{
+	return 2u * act_cap > T && T >= 1024 ? NT_DENSE : NT_SPARSE;
+}
+
 inline int step_threads(const WorldDev &w)
 {
-	const uint32_t T = 1u << w.log_tile;
-	return 2u * w.act_cap > T && T >= 1024 ? NT_DENSE : NT_SPARSE;
+	return step_threads_for(1u << w.log_tile, w.act_cap);
+}
+
+/* Dynamic shared memory of a tile CTA: five agent arrays of act_cap words,
+ * then the cell counters (a word a cell) and the grass (two bytes a cell). */
+inline size_t step_smem(uint32_t T, uint32_t act_cap)
+{
+	return (size_t) act_cap * 5 * sizeof(uint32_t)
+		+ (size_t) T * (sizeof(uint32_t) + sizeof(uint16_t));
 }
 
 template <bool ACT>
@@ -753,8 +772,7 @@ cudaError_t launch_step(const WorldDev &w, const LaunchCfg &lc, uint32_t first,
 	uint32_t count, uint32_t out_base, cudaStream_t s)
 {
 	const uint32_t T = 1u << w.log_tile;
-	const size_t smem = (size_t) w.act_cap * 5 * sizeof(uint32_t)
-		+ (size_t) T * (sizeof(uint32_t) + sizeof(uint16_t));
+	const size_t smem = step_smem(T, w.act_cap);
 	const uint32_t grid = ACT ? (uint32_t) std::max(1, lc.act_tiles) : count;
 	if (step_threads(w) == NT_DENSE) {
 		switch (T / NT_DENSE) {
@@ -806,6 +824,58 @@ cudaError_t enqueue_move_groups(const WorldDev &w, const LaunchCfg &lc,
 {
 	if (count == 0) return cudaSuccess;
 	return launch_step<false>(w, lc, first, count, out_base, s);
+}
+
+int step_ctas_per_sm(uint32_t log_tile, uint32_t act_cap)
+{
+	const uint32_t T = 1u << log_tile;
+	const size_t smem = step_smem(T, act_cap);
+	int n = 0;
+	cudaError_t e;
+	if (step_threads_for(T, act_cap) == NT_DENSE) {
+		switch (T / NT_DENSE) {
+		case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_act<4, NT_DENSE>, NT_DENSE, smem); break;
+		case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_act<8, NT_DENSE>, NT_DENSE, smem); break;
+		case 16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_act<16, NT_DENSE>, NT_DENSE, smem); break;
+		default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_act<32, NT_DENSE>, NT_DENSE, smem); break;
+		}
+	} else {
+		switch (T / NT_SPARSE) {
+		case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_act<4, NT_SPARSE>, NT_SPARSE, smem); break;
+		case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_act<8, NT_SPARSE>, NT_SPARSE, smem); break;
+		case 16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_act<16, NT_SPARSE>, NT_SPARSE, smem); break;
+		case 32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_act<32, NT_SPARSE>, NT_SPARSE, smem); break;
+		default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_act<64, NT_SPARSE>, NT_SPARSE, smem); break;
+		}
+	}
+	if (e != cudaSuccess) {
+		cudaGetLastError();
+		return 0;
+	}
+	return n;
+}
+
+uint32_t grow_act_cap(uint32_t log_tile, uint32_t act_cap)
+{
+	const uint32_t T = 1u << log_tile;
+	if (set_step_smem_limits(step_smem(T, 2 * T)) != cudaSuccess) {
+		cudaGetLastError();
+		return act_cap;
+	}
+	/* the record cache of the move phase needs 2 act_cap <= T and
+	 * 2 act_cap <= 2048 (pp_fused.cu E1) */
+	auto cache_ok = [&](uint32_t a) { return 2u * a <= T && 2u * a <= 2048u; };
+	const int occ = step_ctas_per_sm(log_tile, act_cap);
+	const int nt = step_threads_for(T, act_cap);
+	const bool cached = cache_ok(act_cap);
+	if (occ <= 0) return act_cap;
+	for (uint32_t a = act_cap + 32; a <= 2 * T; a += 32) {
+		if (step_threads_for(T, a) != nt || (cached && !cache_ok(a))
+			|| step_ctas_per_sm(log_tile, a) < occ)
+			break;
+		act_cap = a;
+	}
+	return act_cap;
 }
 
 cudaError_t set_step_smem_limits(size_t bytes)

@@ -98,6 +98,15 @@ cudaError_t enqueue_fused_bases(const WorldDev &w, const LaunchCfg &lc,
 
 cudaError_t set_step_smem_limits(size_t bytes);
 
+/* Fused act CTAs per SM for tiles of 2^log_tile cells with act_cap agents
+ * in shared memory (0 if the query fails). */
+int step_ctas_per_sm(uint32_t log_tile, uint32_t act_cap);
+
+/* The largest act_cap (in steps of 32) above the given one that keeps its
+ * CTAs per SM, its CTA size and its move-phase record cache: more agents
+ * held in shared memory at no cost in occupancy. */
+uint32_t grow_act_cap(uint32_t log_tile, uint32_t act_cap);
+
 /* Bounded look-back self-test over n chunks (chunk `stall` never
  * publishes; `limit` polls per wait). */
 cudaError_t launch_lookback_selftest(uint64_t *lb, uint32_t *ticket, uint32_t *err,

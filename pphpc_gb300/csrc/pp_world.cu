@@ -206,6 +206,10 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	/* the fused act keeps a byte per output (at most 2 act_cap) in the
 	 * tile's 4 T bytes of cell counters */
 	act_cap = std::min<uint32_t>(act_cap, 2 * T);
+	/* fused pipeline: the shared memory the chosen act_cap leaves unused at
+	 * its CTAs per SM holds more agents (12800^2, 2048-cell tiles: 512 ->
+	 * 576, so fewer tiles at the population peak take the crowded path) */
+	if (cfg.fused && cfg.act_cap == 0) act_cap = grow_act_cap(log_tile, act_cap);
 	w_.act_cap = act_cap;
 
 	const size_t cap = cfg.cap;
