@@ -156,7 +156,9 @@ __device__ __forceinline__ uint32_t step_excl_scan(uint32_t v, uint32_t *total)
  * thread per agent (as the sort pipeline's act); E0 output offsets and
  * stats; E1 move draws and per-class counts;
  * one warp allocates the tile's groups and posts them to the destination
- * tiles' inboxes; E2 records into the groups; per-tile stats. */
+ * tiles' inboxes; E2 records into the groups; per-tile stats. (!ACT: the
+ * bucket read and counted per cell, the same counting sort with each
+ * cell's agents in creation order, then E1 and E2 on every agent.) */
 template <int CPT, int NT, bool ACT>
 __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 	uint32_t out_base, uint32_t *sm)
