@@ -1,8 +1,8 @@
 """Full-size runs against oracle fixtures made on the CPU
 (tests/golden/make_golden.py large): the 12800x12800 v1 workload through its
-population peak (rows 0..300 and the final state), and every class of the
-64-run batched mix for all 4000 iterations, plain, batched in the real mix,
-and served."""
+population peak (rows 0..300 and the state after them) and for all 4000
+iterations, in both pipelines, and every class of the 64-run batched mix for
+all 4000 iterations, plain, batched in the real mix, and served."""
 import hashlib
 import os
 
@@ -107,10 +107,11 @@ def test_served_world_holds_mix_classes():
     srv.close()
 
 
-def test_12800_full_run_rows():
+@pytest.mark.parametrize("sort_pipeline", [False, True], ids=["fused", "sort"])
+def test_12800_full_run_rows(sort_pipeline):
     """The 12800x12800 v1 workload (seed 2, pool 5x) against every row the
     oracle's full-length fixture holds (all 4000 iterations, or the first
-    rows of an interrupted generation)."""
+    rows of an interrupted generation), in both iteration pipelines."""
     path = os.path.join(GOLDEN, "stats_12800v1_s2_full.npz")
     if not os.path.exists(path):
         pytest.skip("full-length fixture not generated (make_golden.py large)")
@@ -118,5 +119,6 @@ def test_12800_full_run_rows():
     want = g["rows"]
     k = int(g["iters_done"][0])
     assert len(want) == k + 1 and k >= 500
-    got = rows_array(pp.run(p, seed, k, max_agents=int(g["pool"][0])))
+    got = rows_array(pp.run(p, seed, k, max_agents=int(g["pool"][0]),
+                            sort_pipeline=sort_pipeline))
     assert first_diff(got, want) is None
