@@ -327,14 +327,17 @@ def run_ours(args, dist):
     cap = (5 if args.params == "v1" else 40) * n0
     K, W = args.steps, args.warmup
 
-    # -- launch geometry from the autotuner (or --tile-cells) --
+    # -- launch geometry from the autotuner (or --tile-cells, or the sort
+    # pipeline forced by --sort-pipeline for profiling its kernels) --
     tuning = None
-    if args.tile_cells == 0:
+    auto = args.tile_cells == 0 and not args.sort_pipeline
+    if auto:
         tuning = pp.autotune(p, SEED, cap, dev)
+    sim_kw = dict(device=dev, max_agents=cap, tile_cells=args.tile_cells, autotune=auto,
+                  sort_pipeline=args.sort_pipeline)
 
     # -- device-timed throughput (state resident in HBM) --
-    sim = pp.Simulation(p, SEED, device=dev, max_agents=cap, tile_cells=args.tile_cells,
-                        autotune=args.tile_cells == 0)
+    sim = pp.Simulation(p, SEED, **sim_kw)
     sim.step(W)
     clocks = ClockSampler(dev)
     clocks.start()
@@ -363,7 +366,8 @@ def run_ours(args, dist):
     spec_b, P = spec_bytes_per_iter(cells, n_avg)
     launch_s = (tot_ms / launches) / 1e3
     achieved = spec_b / launch_s / 1e9
-    traffic = kernel_traffic(name, cells, n_avg)
+    # the committed DRAM figures are the fused pipeline's kernels
+    traffic = None if args.sort_pipeline else kernel_traffic(name, cells, n_avg)
     step_bytes = sum(k[3] for k in kernels) / prof_iters
     step_ms = sum(k[2] for k in kernels) / prof_iters
     timed_spec_bytes = sum(spec_bytes_per_iter(cells, r.sheep + r.wolves)[0] for r in rows)
@@ -376,8 +380,7 @@ def run_ours(args, dist):
     for _ in range(E2E_JOBS):
         dist.barrier()
         t0 = time.perf_counter()
-        sim2 = pp.Simulation(p, SEED, device=dev, max_agents=cap, tile_cells=args.tile_cells,
-                             autotune=args.tile_cells == 0)
+        sim2 = pp.Simulation(p, SEED, **sim_kw)
         rows0 = [sim2.stats0()]
         rows_e = sim2.step(K)
         h2d, d2h = sim2.io_bytes()
@@ -395,7 +398,8 @@ def run_ours(args, dist):
         "vs_baseline": None, "dtype": "u32", "data": "synthetic (model's own seeded init)",
         "config": config_of(args, dist.world),
         "setup": {"agent_pool": cap, "state": "uint32 SoA agents, uint16 grass",
-                  "geometry": tuning if tuning else {"tile_cells": args.tile_cells}},
+                  "geometry": tuning if tuning else {"tile_cells": args.tile_cells,
+                                                     "sort_pipeline": args.sort_pipeline}},
         "iters_per_s": iters_per_s,
         "e2e": {"value": e2e_value, "unit": "agent-steps/s",
                 "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
@@ -462,7 +466,8 @@ def full_run(args, dist, p, cap):
     import pphpc_gb300 as pp
     dev = dist.local
     kw = dict(device=dev, max_agents=cap, tile_cells=args.tile_cells,
-              autotune=args.tile_cells == 0)
+              autotune=args.tile_cells == 0 and not args.sort_pipeline,
+              sort_pipeline=args.sort_pipeline)
     dist.barrier()
     t0 = time.perf_counter()
     sim = pp.Simulation(p, SEED, **kw)
@@ -705,6 +710,9 @@ def main():
                     help="requests of the served stream (0 = skip the leg)")
     ap.add_argument("--side", type=int, default=12800,
                     help="grid side of the plain workload (agents scale by area)")
+    ap.add_argument("--sort-pipeline", action="store_true",
+                    help="run the plain workload on the per-iteration sort pipeline "
+                         "(for profiling its kernels; no autotuning)")
     ap.add_argument("--params", choices=["v1", "v2"], default="v1",
                     help="parameter set of the plain workload")
     ap.add_argument("--tile-cells", type=int, default=0,
