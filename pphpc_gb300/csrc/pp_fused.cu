@@ -170,6 +170,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 	__shared__ uint32_t s_tbl[CLS_FOREIGN];
 	__shared__ uint32_t s_ccnt[NCLS + 1], s_cpos[NCLS + 1];   /* + a discard slot */
 	__shared__ uint32_t s_xbase, s_fail;
+	__shared__ uint64_t red[5][NT / 32];    /* per-warp partial stats */
 
 	const uint32_t tid = threadIdx.x, lane = tid & 31;
 	const uint32_t c0 = tile << w.log_tile;
@@ -279,9 +280,13 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 	 * memory and once for a crowded tile's global scratch: each copy then
 	 * addresses one memory space directly (shared loads and stores with
 	 * 32-bit addresses) instead of through generic pointers. */
-	auto phases = [&](auto smem_tag, uint32_t *UK, uint32_t *UV, uint32_t *PERM,
+	auto phases = [&](auto smem_tag, auto split_tag, uint32_t *UK, uint32_t *UV, uint32_t *PERM,
 		uint32_t *LK, uint32_t *LV) {
 		constexpr bool in_smem = decltype(smem_tag)::value;
+		/* the move phase's record cache spread over the dead counter and
+		 * grass words and the permutation array's tail (tiles whose 2 act_cap
+		 * outputs do not fit the counters) */
+		constexpr bool split = decltype(split_tag)::value;
 		uint32_t *LP = UK, *LD = UV;      /* priorities / dice, then offsets / kids */
 
 		uint32_t eats = 0;
@@ -549,16 +554,27 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 			en = nb ? (LD[j] & KID_ENERGY) : (LV[j] & ENERGY_MASK);
 		};
 
-		/* ---- E1: move draws of the outputs, per-class counts; with room in
-		 * the cell counters' words (2 act_cap <= T) and offsets that fit 11
-		 * bits (2 act_cap <= 2048), each output's cell in its destination
-		 * tile (bits 0-12), direction (13-15; DIR_DROPPED for an output
-		 * counted nowhere), class (16-20) and offset in its class's group
-		 * (21-31) are kept for E2, else only its direction ---- */
+		/* ---- E1: move draws of the outputs, per-class counts; with room for
+		 * a word per output and offsets that fit 11 bits (at most 2048
+		 * outputs), each output's cell in its destination tile (bits 0-12),
+		 * direction (13-15; DIR_DROPPED for an output counted nowhere),
+		 * class (16-20) and offset in its class's group (21-31) are kept for
+		 * E2, else only its direction. The room: the cell counters' words
+		 * (T, enough when 2 act_cap <= T); in split tiles the counters, the
+		 * grass words after them (T / 2 words, dead after the actions) and
+		 * the permutation array past the output map, per tile as its
+		 * outputs need ---- */
 		bool bad = false;
-		const bool cache = in_smem && 2u * w.act_cap <= (uint32_t) (CPT * NT)
-			&& 2u * w.act_cap <= 2048u;
+		constexpr uint32_t DEST_A = CPT * NT + CPT * NT / 2;
+		const uint32_t dest_b0 = (total + 1) / 2;    /* words of the output map */
+		const bool cache = in_smem && (split
+			? total <= 2048u && total <= DEST_A + (w.act_cap - dest_b0)
+			: 2u * w.act_cap <= 2048u);
 		uint32_t *DEST = scnt;
+		auto dest = [&](uint32_t o) -> uint32_t & {
+			if (!split || o < DEST_A) return DEST[o];
+			return PERM[dest_b0 + (o - DEST_A)];
+		};
 		for (uint32_t o = tid; o < total; o += NT) {
 			uint32_t j, nb, en, rank;
 			output(o, j, nb, en, rank);
@@ -584,7 +600,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 			}
 			const uint32_t off = warp_agg_add(s_ccnt, cls);
 			if (cache)
-				DEST[o] = cls == NCLS ? DIR_DROPPED << REC_DIR_SHIFT
+				dest(o) = cls == NCLS ? DIR_DROPPED << REC_DIR_SHIFT
 					: klo | (code << REC_DIR_SHIFT) | (cls << 16) | (off << 21);
 			else DIR[o] = (uint8_t) code;
 		}
@@ -632,7 +648,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 				const uint32_t tb = LV[j] & TYPE_BIT;
 				uint32_t key, val, cls;
 				if (cache) {
-					const uint32_t d = DEST[o];
+					const uint32_t d = dest(o);
 					const uint32_t code = (d >> REC_DIR_SHIFT) & 7u;
 					cls = (d >> 16) & 31u;
 					key = (d & 0xffffu) | (rank << REC_RANK_SHIFT);
@@ -675,7 +691,6 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 		/* ---- per-tile partial stats (ACT); the tile's eating events go to the
 		 * run's regrowth histogram slot of iteration t + restart ---- */
 		if (ACT) {
-			__shared__ uint64_t red[5][NT / 32];
 			const uint32_t wid = tid >> 5;
 			const uint32_t sw = warp_sum(sheep | (wolves << 16));
 			const uint32_t ew = warp_sum(eats);
@@ -713,11 +728,15 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 		}
 	};
 	if (in_smem) {
-		phases(std::true_type{}, sk, sv, sperm, sp, sd);
+		if (2u * w.act_cap <= (uint32_t) (CPT * NT))
+			phases(std::true_type{}, std::false_type{}, sk, sv, sperm, sp, sd);
+		else
+			phases(std::true_type{}, std::true_type{}, sk, sv, sperm, sp, sd);
 	} else {
 		const uint32_t xb = s_xbase;
-		phases(std::false_type{}, w.scratch_prio + xb, w.scratch_kid + xb,
-			w.scratch_perm + 3ull * xb, w.scratch_key + xb, w.scratch_val + xb);
+		phases(std::false_type{}, std::false_type{}, w.scratch_prio + xb,
+			w.scratch_kid + xb, w.scratch_perm + 3ull * xb, w.scratch_key + xb,
+			w.scratch_val + xb);
 	}
 }
 
