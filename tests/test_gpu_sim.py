@@ -85,6 +85,28 @@ def test_crowded_cells(sort_pipeline):
                max_agents=400_000, sort_pipeline=sort_pipeline)
 
 
+def test_dense_tiles_record_cache_paths():
+    """512-cell tiles of a dense world (act_cap 2 T, so the move phase's
+    record cache is spread over the dead counter, grass and permutation
+    words), every acting agent reproducing: tiles pass from the spread cache
+    (outputs that fit) through the uncached record writes (about twice as
+    many outputs as agents, more than the spread words hold) to the crowded
+    path as the population doubles."""
+    p = params(0, 2, gx=64, gy=64, sheep=3000, wolves=1500, iters=8)
+    p.sheep_reproduce_threshold = 0
+    p.sheep_reproduce_prob = 100
+    p.wolves_reproduce_threshold = 0
+    p.wolves_reproduce_prob = 100
+    pool = 2_000_000
+    # agents a tile at the acts of iterations 1, 2, 3: about 560 (outputs
+    # ~970, cached), 970 (outputs ~1650, uncached), 1650 (crowded)
+    st = orc.State(p, 7, capacity=pool)
+    want = np.array([st.stats()] + [st.step() for _ in range(p.iters)], np.uint64)
+    st.close()
+    got = rows_array(pp.run(p, 7, tile_cells=512, max_agents=pool))
+    assert first_diff(got, want) is None
+
+
 def test_pool_overflow_at_scale_is_refused():
     """A pool far below the population: 3200^2 v2 grows to about 27 times
     its initial agents while the pool holds 5 times, and on 512-cell tiles most
