@@ -641,7 +641,7 @@ def run_served(args, dist):
         if not pending:
             time.sleep(max(0.0, reqs[nxt][0] - now))
             continue
-        srv.poll(16)
+        srv.poll(args.served_poll)
         now = time.perf_counter() - t0
         for rid in srv.finished():
             ev = srv.status(rid)
@@ -708,6 +708,8 @@ def main():
     ap.add_argument("--workload", choices=["plain", "served", "configs"], default="plain")
     ap.add_argument("--served-requests", type=int, default=1000,
                     help="requests of the served stream (0 = skip the leg)")
+    ap.add_argument("--served-poll", type=int, default=16,
+                    help="iterations the served loop advances per poll")
     ap.add_argument("--side", type=int, default=12800,
                     help="grid side of the plain workload (agents scale by area)")
     ap.add_argument("--sort-pipeline", action="store_true",
