@@ -626,7 +626,7 @@ def run_served(args, dist):
         iters = rng.randint(500, 4000)
         reqs.append((t_arr, scaled_params(pp, side, version, iters), 1000 + i))
     srv = pp.Server(mem_budget_bytes=150 << 30, max_runs=1024, pool_factor=POOL_FACTOR,
-                    stats_chunk=64, device=dist.local)
+                    stats_chunk=64, device=dist.local, tile_cells=args.served_tile)
     pending = {}
     lat = []
     steps = 0
@@ -708,6 +708,8 @@ def main():
     ap.add_argument("--workload", choices=["plain", "served", "configs"], default="plain")
     ap.add_argument("--served-requests", type=int, default=1000,
                     help="requests of the served stream (0 = skip the leg)")
+    ap.add_argument("--served-tile", type=int, default=0,
+                    help="cells per tile of the served world (0 = the library's default)")
     ap.add_argument("--served-poll", type=int, default=16,
                     help="iterations the served loop advances per poll")
     ap.add_argument("--side", type=int, default=12800,

@@ -379,7 +379,7 @@ typedef struct pp_serve_opts {
 	uint32_t stats_chunk;       /* iterations between stats streaming     */
 	uint32_t ss_from;           /* focal measures' steady state: t > ss_from */
 	uint32_t agent_size;        /* energy field of every run, as pp_opts.agent_size */
-	uint32_t tile_cells;        /* cells per tile: 512, 1024 (0 = default) or 2048 */
+	uint32_t tile_cells;        /* cells per tile: 512, 1024 or 2048 (0 = default, 2048) */
 } pp_serve_opts;
 
 void pp_serve_opts_default(pp_serve_opts *opts);

@@ -98,7 +98,10 @@ extern "C" int pp_serve_create(const pp_serve_opts *opts, pp_server **out)
 	 * (three key/value arrays for sorting a new run's agents, two group
 	 * buffers of three slots per agent, seven scratch words for crowded
 	 * tiles, sort look-back). Cells are bounded by the 2^31 key space. */
-	const uint32_t T = o.tile_cells ? o.tile_cells : 1024;
+	/* 2048-cell tiles by default: on a 1000-request stream of 100^2 to
+	 * 3200^2 runs they served 2.17e10 agent-steps/s against 1.86e10 on
+	 * 1024-cell tiles and 2.01e10 on 512 */
+	const uint32_t T = o.tile_cells ? o.tile_cells : 2048;
 	const uint64_t tile_bytes = T * 2ull + 610;
 	uint64_t budget = o.mem_budget_bytes;
 	uint64_t cell_bytes = budget / 8;
