@@ -193,6 +193,7 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 		dbase_t = w.dbase[tile];
 	}
 	const uint32_t g = w.ctr->giter + 1;
+	const uint32_t err_now = ACT ? w.ctr->err : 0u;
 	const uint32_t pin = g & 1, pout = ACT ? (g + 1) & 1 : g & 1;
 	/* the run's parameters, copied to shared memory: they are read in every
 	 * phase, and through a reference into global memory they would be
@@ -205,9 +206,14 @@ __device__ __forceinline__ void step_tile(const WorldDev &w, uint32_t tile,
 		reinterpret_cast<uint32_t *>(&s_run)[tid] = reinterpret_cast<const uint32_t *>(&grun)[tid];
 	const RunDev &run = s_run;
 	const uint32_t t = g - grun.start_giter;
-	if (ACT && !run_live(grun, t)) {
+	/* a world whose agent pool has overflowed is failed (the host returns
+	 * PP_OUT_OF_RESOURCES at its next check): its later acts do nothing,
+	 * so a run that overflowed early does not grind through its remaining
+	 * iterations on a corrupted state */
+	if (ACT && (!run_live(grun, t) || (err_now & ERRF_OVERFLOW))) {
 		cp_async_wait_all();
-		/* finished run or free tile space: nothing survives, no stats */
+		/* finished run, free tile space or a failed world: nothing
+		 * survives, no stats */
 		if (tid == 0) w.inbox_n[(size_t) pin * w.n_tiles + tile] = 0;
 		if (tid < 8) w.part[(size_t) tile * 8 + tid] = 0;
 		return;

@@ -266,8 +266,11 @@ __global__ void __launch_bounds__(ACT_THREADS, 5) k_act(WorldDev w,
 	const uint32_t g = w.ctr->giter + 1;
 	const RunDev &run = w.runs[w.tile_run[tile]];
 	const uint32_t t = g - run.start_giter;
-	if (!run_live(run, t)) {
-		/* finished run or free tile space: no agents survive, no stats */
+	/* a world whose agent pool has overflowed is failed (the host returns
+	 * PP_OUT_OF_RESOURCES at its next check): its later acts do nothing */
+	if (!run_live(run, t) || (w.ctr->err & ERRF_OVERFLOW)) {
+		/* finished run, free tile space or a failed world: no agents
+		 * survive, no stats */
 		if (tid == 0) {
 			w.rstart[tile] = 0;
 			w.rcnt[tile] = 0;

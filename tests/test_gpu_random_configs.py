@@ -13,7 +13,7 @@ from common import rows_array, first_diff
 
 pytestmark = pytest.mark.gpu
 
-N_CASES = 40
+N_CASES = 120
 
 
 def _case(k):
