@@ -95,9 +95,9 @@ extern "C" int pp_serve_create(const pp_serve_opts *opts, pp_server **out)
 	srv->opts = o;
 	/* Budget split: a tile costs 2 B per cell (grass) plus ~610 B of
 	 * per-tile tables (inboxes, offsets, partial stats), an agent slot 101 B
-	 * (three key/value arrays for sorting a new run's agents, two group
-	 * buffers of three slots per agent, seven scratch words for crowded
-	 * tiles, sort look-back). Cells are bounded by the 2^31 key space. */
+	 * (a new run's agents in creation order and bucketed by tile, 24 B; two
+	 * group buffers of three slots per agent; seven scratch words for
+	 * crowded tiles; sort look-back). Cells are bounded by the 2^31 key space. */
 	/* 2048-cell tiles by default: on a 1000-request stream of 100^2 to
 	 * 3200^2 runs they served 2.17e10 agent-steps/s against 1.86e10 on
 	 * 1024-cell tiles and 2.01e10 on 512 */

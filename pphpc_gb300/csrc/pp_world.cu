@@ -308,8 +308,8 @@ int World::create(const std::vector<RunSpec> &runs, const WorldConfig &cfg_in)
 	lc_.act_tiles = (int) std::max<uint32_t>(tile_hi_, 1);
 
 	/* Initial state: grass, then every run's agents in creation order into
-	 * B at the run's base; fused pipeline: bucketed by tile into A and
-	 * moved once; sort pipeline: sorted by cell into the region buffer, the
+	 * B at the run's base; fused pipeline: bucketed by tile and moved
+	 * once; sort pipeline: sorted by cell into the region buffer, the
 	 * tiles' regions and dense bases (runs occupy increasing cell ranges,
 	 * so either way each run's agents stay at its base); stats row 0. */
 	std::vector<PPStatistics> resumed_row0(runs.size());
