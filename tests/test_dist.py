@@ -75,3 +75,21 @@ def test_reference_arm_under_torchrun_prints_one_line():
     import bench
     a = argparse.Namespace(side=200, params="v1", steps=2, warmup=3)
     assert d["config"] == bench.config_of(a, 2)
+
+
+def test_workload_options_name_the_workload():
+    """The plain workload's options: --side scales the grid (agents by area),
+    --params picks the parameter set, and both arms' config objects say so."""
+    import argparse
+    sys.path.insert(0, ROOT)
+    import bench
+    a = argparse.Namespace(side=12800, params="v1", steps=20, warmup=5)
+    wl, name = bench.workload_dict(a)
+    assert name == "pphpc-12800x12800-v1" and wl == bench.WORKLOAD
+    a = argparse.Namespace(side=3200, params="v2", steps=3, warmup=300)
+    wl, name = bench.workload_dict(a)
+    assert name == "pphpc-3200x3200-v2"
+    assert (wl["grid_x"], wl["init_sheep"], wl["init_wolves"]) == (3200, 409600, 204800)
+    assert wl["sheep_gain_from_food"] == bench.V2["sheep_gain_from_food"]
+    c = bench.config_of(a, 1)
+    assert c["params"] == "v2" and c["timed_iterations"] == "301..303"
